@@ -1,0 +1,759 @@
+// C ABI of galario_gb300: the drop-in boundary for galario's
+// sampleImage / chi2Image / sampleProfile / chi2Profile (reference
+// src/galario_py.h:30-46) plus the expert stages and runtime helpers
+// (src/galario.h:24-59).  See include/galario_gb300.h for the contract.
+//
+// Every entry point returns a status (GALARIO_OK, GALARIO_EINVAL,
+// GALARIO_ENOMEM, GALARIO_ERUNTIME) and leaves a message for the calling
+// thread in galario_last_error(), the way the reference throws
+// std::invalid_argument / std::bad_alloc / std::runtime_error
+// (src/galario.cpp:89-198) and Cython maps them to ValueError / MemoryError /
+// RuntimeError (python/galario_defs.pxd:24-46).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/galario_gb300.h"
+#include "gb_internal.cuh"
+
+namespace gbg {
+namespace {
+
+thread_local std::string g_msg;
+thread_local int g_tpb = 16;  // galario threads(): accepted for API compatibility
+
+struct InvalidArg : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+struct OutOfMemory : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+void cuda_check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return;
+    cudaGetLastError();  // clear sticky-free errors
+    if (e == cudaErrorMemoryAllocation) throw OutOfMemory(std::string("cuda out of memory in ") + what);
+    if (e == cudaErrorInitializationError || e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+        throw std::runtime_error("Error in cuda: Could not initialize cuda. Is a CUDA GPU available at all?");
+    throw std::runtime_error(std::string("Error in cuda (") + what + "): " + cudaGetErrorString(e));
+}
+#define CK(x) cuda_check((x), #x)
+
+template <class F> int guarded(F&& f) {
+    try {
+        f();
+        return GALARIO_OK;
+    } catch (const InvalidArg& e) {
+        g_msg = e.what();
+        return GALARIO_EINVAL;
+    } catch (const OutOfMemory& e) {
+        g_msg = e.what();
+        return GALARIO_ENOMEM;
+    } catch (const std::bad_alloc&) {
+        g_msg = "std::bad_alloc";
+        return GALARIO_ENOMEM;
+    } catch (const std::exception& e) {
+        g_msg = e.what();
+        return GALARIO_ERUNTIME;
+    }
+}
+
+// reference CHECK_INPUT / CHECK_INPUTXY, src/galario.cpp:101-111
+void check_input(long long nx) {
+    if (nx < 2)
+        throw InvalidArg("Error in check input image: x dimension = " + std::to_string(nx) + " is less than 2");
+    if (nx % 2 != 0) throw InvalidArg("Error in check input image: x dimension = " + std::to_string(nx) + " is odd");
+}
+void check_square(long long nx, long long ny) {
+    if (nx != ny)
+        throw InvalidArg("Error in check input image: Expect a square image but got shape (" + std::to_string(nx) +
+                         ", " + std::to_string(ny) + ")");
+    check_input(nx);
+}
+void check_nd(int nd) {
+    if (nd < 0) throw InvalidArg("Error: negative number of visibilities " + std::to_string(nd));
+}
+
+// ---------------------------------------------------------------------------
+// per-device context: stream, grow-only device buffers, twiddle tables
+// ---------------------------------------------------------------------------
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    void* get(size_t bytes) {
+        if (bytes == 0) bytes = 16;
+        if (bytes > cap) {
+            if (p) cudaFree(p);
+            p = nullptr;
+            cap = 0;
+            CK(cudaMalloc(&p, bytes));
+            cap = bytes;
+        }
+        return p;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct Ctx {
+    int device = 0;
+    std::mutex mu;
+    cudaStream_t stream = nullptr;
+    DevBuf state, partials, img, prof, u, v, re, im, w, vis, zt, win, urot, vrot;
+    std::map<std::pair<int, int>, void*> tw;  // (N, sizeof(T)) -> table
+    DevState* host_state = nullptr;           // pinned mirror of DevState
+
+    void init(int dev) {
+        device = dev;
+        CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        CK(cudaMallocHost(&host_state, sizeof(DevState)));
+    }
+    void release_all() {
+        DevBuf* bufs[] = {&state, &partials, &img, &prof, &u, &v, &re, &im, &w, &vis, &zt, &win, &urot, &vrot};
+        for (DevBuf* b : bufs) b->release();
+        for (auto& kv : tw) cudaFree(kv.second);
+        tw.clear();
+    }
+    // twiddles exp(-2 pi i m / N), m in [0, N), from long double, cached per (N, precision)
+    template <typename T> const C2<T>* twiddles(int N) {
+        auto key = std::make_pair(N, (int)sizeof(T));
+        auto it = tw.find(key);
+        if (it != tw.end()) return static_cast<const C2<T>*>(it->second);
+        std::vector<C2<T>> h((size_t)N);
+        const long double two_pi = 6.283185307179586476925286766559005768L;
+        for (int m = 0; m < N; ++m) {
+            // exact symmetry folding keeps the argument small: angle = 2 pi m / N
+            long double a = -two_pi * (long double)m / (long double)N;
+            h[(size_t)m].x = (T)cosl(a);
+            h[(size_t)m].y = (T)sinl(a);
+        }
+        void* d = nullptr;
+        CK(cudaMalloc(&d, sizeof(C2<T>) * (size_t)N));
+        CK(cudaMemcpy(d, h.data(), sizeof(C2<T>) * (size_t)N, cudaMemcpyHostToDevice));
+        tw[key] = d;
+        return static_cast<const C2<T>*>(d);
+    }
+};
+
+std::mutex g_ctx_mu;
+std::map<int, Ctx*> g_ctx;
+
+Ctx& ctx() {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    auto it = g_ctx.find(dev);
+    if (it != g_ctx.end()) return *it->second;
+    Ctx* c = new Ctx();
+    c->init(dev);
+    g_ctx[dev] = c;
+    return *c;
+}
+
+template <typename T> T* as(DevBuf& b, size_t count) { return static_cast<T*>(b.get(sizeof(T) * count)); }
+
+void h2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    if (bytes) CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+}
+void d2h(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+    if (bytes) CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+}
+
+// Read back DevState and turn device-side error bits into exceptions.
+void finish(Ctx& c, DevState* st_d) {
+    d2h(c.host_state, st_d, sizeof(DevState), c.stream);
+    CK(cudaStreamSynchronize(c.stream));
+    const DevState& h = *c.host_state;
+    if (h.err & ERR_UV_NONFINITE)
+        throw InvalidArg("Error in interpolate: u or v is not finite (first at index " +
+                         std::to_string((long long)h.err_index - 1) + ")");
+    if (h.err & ERR_UV_OUTSIDE)
+        throw InvalidArg(
+            "Error in interpolate: a (u, v) point lies outside the image spectrum, |u|/duv or |v|/duv is too large "
+            "for nxy (first at index " + std::to_string((long long)h.err_index - 1) +
+            "); use check=True or a larger nxy / smaller dxy");
+    if (h.err & ERR_WINDOW) throw std::runtime_error("Error in interpolate: internal spectrum window error");
+    if (h.err) throw std::runtime_error("Error: device reported error bits " + std::to_string(h.err));
+}
+
+// central pixel of the swept image (reference create_image_d, src/galario.cpp:1135-1153)
+double central_pixel(const double* I, int nr, double Rmin, double dR, double dxy) {
+    const int iIN = (int)std::floor((dxy / 2 - Rmin) / dR);
+    if (iIN < 0 || iIN + 1 >= nr)
+        throw InvalidArg("Error in create image: the intensity profile (nr = " + std::to_string(nr) +
+                         ") does not reach the edge of the central pixel (needs index " + std::to_string(iIN + 1) +
+                         ")");
+    double flux = 0.;
+    for (int i = 1; i < iIN; ++i) flux += (Rmin + dR * i) * I[i];
+    flux *= 2.;
+    flux += Rmin * I[0] + (Rmin + iIN * dR) * I[iIN];
+    flux *= dR;
+    const double I_interp = (I[iIN + 1] - I[iIN]) / dR * (dxy / 2. - (Rmin + dR * iIN)) + I[iIN];
+    flux += ((Rmin + iIN * dR) * I[iIN] + dxy / 2. * I_interp) * (dxy / 2. - (Rmin + iIN * dR));
+    const double area = std::pow(dxy / 2., 2) - std::pow(Rmin, 2);
+    return dxy * dxy * flux / area;
+}
+
+// reference CHECK_CENTRAL_PIXEL, src/galario.cpp:113-121
+void check_central_pixel(double dxy, double Rmin, double dR) {
+    const double ratio = (dxy / 2. - Rmin) / dR;
+    if (ratio < 5)
+        throw InvalidArg(
+            "Error in create image: Expect (dxy/2-Rmin)/dR > 5, i.e. dR small enough to ensure reliable "
+            "interpolation the inside central pixel but got (dxy/2-Rmin)/dR = " + std::to_string(ratio) +
+            ". Try reducing dR.");
+}
+
+struct ProfileGeom {
+    int rmax;
+    double central;
+};
+
+template <typename T>
+ProfileGeom profile_geom(const T* I_host, int nr, double Rmin, double dR, double dxy, int nxy) {
+    check_central_pixel(dxy, Rmin, dR);
+    if (nr < 2) throw InvalidArg("Error in create image: the intensity profile needs at least 2 samples");
+    std::vector<double> Id((size_t)nr);
+    for (int i = 0; i < nr; ++i) Id[(size_t)i] = (double)I_host[i];
+    ProfileGeom g;
+    g.central = central_pixel(Id.data(), nr, Rmin, dR, dxy);
+    long long r = (long long)std::ceil((Rmin + nr * dR) / dxy);
+    g.rmax = (int)(r < nxy / 2 ? r : nxy / 2);
+    if (g.rmax < 0) g.rmax = 0;
+    return g;
+}
+
+// ---------------------------------------------------------------------------
+// the pipeline, device side
+// ---------------------------------------------------------------------------
+template <typename T> struct Pipe {
+    using CT = C2<T>;
+    using L = Launch<T>;
+
+    // Enqueue spectrum window + visibility pass.  All pointers are device
+    // pointers.  img != nullptr selects the image path, else the profile path.
+    static void enqueue(Ctx& c, cudaStream_t s, int N, double duv, const T* img, const T* prof, int nr, double Rmin,
+                        double dR, double dxy, double inc, const ProfileGeom* pg, double v_origin, double dRA,
+                        double dDec, double PA, int nd, const T* u, const T* v, const T* re, const T* im, const T* w,
+                        CT* vis_out, bool chi2, double* chi2_out, DevState* st, bool have_extent) {
+        const int C = N / 2 + 1;
+        const CT* tw = c.twiddles<T>(N);
+        CT* zt = as<CT>(c.zt, (size_t)C * N);
+        CT* win = as<CT>(c.win, (size_t)C * N);
+        double* partials = as<double>(c.partials, (size_t)L::vis_grid(nd > 0 ? nd : 1));
+        if (!have_extent) CK(L::extent(u, v, nd, st, s));
+        int band0 = 0, band1 = N;
+        if (img) {
+            CK(L::rows_image(img, N, tw, zt, -1, st, duv, true, s));
+        } else {
+            band0 = N / 2 - pg->rmax;
+            band1 = N / 2 + pg->rmax;
+            CK(L::rows_profile(prof, nr, Rmin, dR, dxy, std::cos(inc), pg->rmax, pg->central, N, tw, zt, st, duv, s));
+        }
+        // window layout: column k at win + k*N, rows [r0, r0+W) contiguous
+        CK(L::cols(zt, N, band0, band1, tw, win, 1, N, -1, -1, -1, st, duv, true, s));
+        typename L::VisArgs a;
+        a.spec = win;
+        a.s_row = 1;
+        a.s_col = N;
+        a.nrow = N;
+        a.ncol = C;
+        a.host_K = a.host_r0 = a.host_W = -1;
+        a.duv = duv;
+        a.v_origin = v_origin;
+        a.rotate = (PA != 0.);
+        a.cos_pa = a.rotate ? std::cos(PA) : 1.;
+        a.sin_pa = a.rotate ? std::sin(PA) : 0.;
+        // rotated offsets, computed on the host as in the reference (:1305)
+        double dra = dRA, ddec = dDec;
+        if (a.rotate) {
+            dra = dRA * a.cos_pa - dDec * a.sin_pa;
+            ddec = dRA * a.sin_pa + dDec * a.cos_pa;
+        }
+        a.dra = dra;
+        a.ddec = ddec;
+        a.phase = !(dra == 0. && ddec == 0.);
+        a.u = u;
+        a.v = v;
+        a.re = re;
+        a.im = im;
+        a.w = w;
+        a.nd = nd;
+        a.vis_out = vis_out;
+        a.partials = chi2 ? partials : nullptr;
+        a.chi2_out = chi2_out;
+        a.state = st;
+        if (nd > 0) CK(L::vis(a, s));
+    }
+};
+
+template <typename T> struct Api {
+    using CT = C2<T>;
+    using L = Launch<T>;
+
+    static void reject_big(int N) {
+        if ((long long)N * (N / 2 + 1) > (1LL << 40)) throw InvalidArg("Error: image too large");
+    }
+
+    // ---- the four user functions --------------------------------------
+    static void sample_image(int nx, int ny, const T* img, T v_origin, T dRA, T dDec, T duv, T PA, int nd,
+                             const T* u, const T* v, T* vis) {
+        check_input(nx);  // reference sample_image :1364
+        check_square(nx, ny);
+        check_nd(nd);
+        reject_big(nx);
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        cudaStream_t s = c.stream;
+        const int N = nx;
+        T* img_d = as<T>(c.img, (size_t)N * N);
+        T* u_d = as<T>(c.u, (size_t)nd);
+        T* v_d = as<T>(c.v, (size_t)nd);
+        CT* vis_d = as<CT>(c.vis, (size_t)nd);
+        DevState* st = as<DevState>(c.state, 1);
+        h2d(img_d, img, sizeof(T) * (size_t)N * N, s);
+        h2d(u_d, u, sizeof(T) * (size_t)nd, s);
+        h2d(v_d, v, sizeof(T) * (size_t)nd, s);
+        CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
+        Pipe<T>::enqueue(c, s, N, (double)duv, img_d, nullptr, 0, 0, 0, 0, 0, nullptr, (double)v_origin, (double)dRA,
+                         (double)dDec, (double)PA, nd, u_d, v_d, nullptr, nullptr, nullptr, vis_d, false, nullptr, st,
+                         false);
+        d2h(vis, vis_d, sizeof(CT) * (size_t)nd, s);
+        finish(c, st);
+    }
+
+    static void chi2_image(int nx, int ny, const T* img, T v_origin, T dRA, T dDec, T duv, T PA, int nd, const T* u,
+                           const T* v, const T* re, const T* im, const T* w, T* chi2) {
+        check_square(nx, ny);  // reference chi2_image :1559
+        check_nd(nd);
+        reject_big(nx);
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        cudaStream_t s = c.stream;
+        const int N = nx;
+        T* img_d = as<T>(c.img, (size_t)N * N);
+        T* u_d = as<T>(c.u, (size_t)nd);
+        T* v_d = as<T>(c.v, (size_t)nd);
+        T* re_d = as<T>(c.re, (size_t)nd);
+        T* im_d = as<T>(c.im, (size_t)nd);
+        T* w_d = as<T>(c.w, (size_t)nd);
+        DevState* st = as<DevState>(c.state, 1);
+        h2d(img_d, img, sizeof(T) * (size_t)N * N, s);
+        h2d(u_d, u, sizeof(T) * (size_t)nd, s);
+        h2d(v_d, v, sizeof(T) * (size_t)nd, s);
+        h2d(re_d, re, sizeof(T) * (size_t)nd, s);
+        h2d(im_d, im, sizeof(T) * (size_t)nd, s);
+        h2d(w_d, w, sizeof(T) * (size_t)nd, s);
+        CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
+        Pipe<T>::enqueue(c, s, N, (double)duv, img_d, nullptr, 0, 0, 0, 0, 0, nullptr, (double)v_origin, (double)dRA,
+                         (double)dDec, (double)PA, nd, u_d, v_d, re_d, im_d, w_d, nullptr, true, nullptr, st, false);
+        finish(c, st);
+        *chi2 = (T)c.host_state->chi2;
+    }
+
+    static void sample_profile(int nr, const T* I, T Rmin, T dR, T dxy, int nxy, T inc, T dRA, T dDec, T duv, T PA,
+                               int nd, const T* u, const T* v, T* vis) {
+        check_input(nxy);  // reference sample_profile :1409
+        check_nd(nd);
+        reject_big(nxy);
+        ProfileGeom pg = profile_geom<T>(I, nr, Rmin, dR, dxy, nxy);
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        cudaStream_t s = c.stream;
+        const int N = nxy;
+        T* I_d = as<T>(c.prof, (size_t)nr);
+        T* u_d = as<T>(c.u, (size_t)nd);
+        T* v_d = as<T>(c.v, (size_t)nd);
+        CT* vis_d = as<CT>(c.vis, (size_t)nd);
+        DevState* st = as<DevState>(c.state, 1);
+        h2d(I_d, I, sizeof(T) * (size_t)nr, s);
+        h2d(u_d, u, sizeof(T) * (size_t)nd, s);
+        h2d(v_d, v, sizeof(T) * (size_t)nd, s);
+        CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
+        Pipe<T>::enqueue(c, s, N, (double)duv, nullptr, I_d, nr, Rmin, dR, dxy, inc, &pg, 1.0, dRA, dDec, PA, nd, u_d,
+                         v_d, nullptr, nullptr, nullptr, vis_d, false, nullptr, st, false);
+        d2h(vis, vis_d, sizeof(CT) * (size_t)nd, s);
+        finish(c, st);
+    }
+
+    static void chi2_profile(int nr, const T* I, T Rmin, T dR, T dxy, int nxy, T inc, T dRA, T dDec, T duv, T PA,
+                             int nd, const T* u, const T* v, const T* re, const T* im, const T* w, T* chi2) {
+        check_input(nxy);  // reference chi2_profile :1619
+        check_nd(nd);
+        reject_big(nxy);
+        ProfileGeom pg = profile_geom<T>(I, nr, Rmin, dR, dxy, nxy);
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        cudaStream_t s = c.stream;
+        const int N = nxy;
+        T* I_d = as<T>(c.prof, (size_t)nr);
+        T* u_d = as<T>(c.u, (size_t)nd);
+        T* v_d = as<T>(c.v, (size_t)nd);
+        T* re_d = as<T>(c.re, (size_t)nd);
+        T* im_d = as<T>(c.im, (size_t)nd);
+        T* w_d = as<T>(c.w, (size_t)nd);
+        DevState* st = as<DevState>(c.state, 1);
+        h2d(I_d, I, sizeof(T) * (size_t)nr, s);
+        h2d(u_d, u, sizeof(T) * (size_t)nd, s);
+        h2d(v_d, v, sizeof(T) * (size_t)nd, s);
+        h2d(re_d, re, sizeof(T) * (size_t)nd, s);
+        h2d(im_d, im, sizeof(T) * (size_t)nd, s);
+        h2d(w_d, w, sizeof(T) * (size_t)nd, s);
+        CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
+        Pipe<T>::enqueue(c, s, N, (double)duv, nullptr, I_d, nr, Rmin, dR, dxy, inc, &pg, 1.0, dRA, dDec, PA, nd, u_d,
+                         v_d, re_d, im_d, w_d, nullptr, true, nullptr, st, false);
+        finish(c, st);
+        *chi2 = (T)c.host_state->chi2;
+    }
+
+    // ---- device-resident variants (no host copies, no synchronisation) ----
+    static void chi2_profile_device(int nr, const T* I_host, const T* I_d, T Rmin, T dR, T dxy, int nxy, T inc,
+                                    T dRA, T dDec, T duv, T PA, int nd, const T* u_d, const T* v_d, const T* re_d,
+                                    const T* im_d, const T* w_d, double* chi2_d, cudaStream_t s) {
+        check_input(nxy);
+        check_nd(nd);
+        ProfileGeom pg = profile_geom<T>(I_host, nr, Rmin, dR, dxy, nxy);
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        if (!s) s = c.stream;
+        DevState* st = as<DevState>(c.state, 1);
+        CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
+        Pipe<T>::enqueue(c, s, nxy, (double)duv, nullptr, I_d, nr, Rmin, dR, dxy, inc, &pg, 1.0, dRA, dDec, PA, nd,
+                         u_d, v_d, re_d, im_d, w_d, nullptr, true, chi2_d, st, false);
+    }
+
+    static void chi2_image_device(int nx, int ny, const T* img_d, T v_origin, T dRA, T dDec, T duv, T PA, int nd,
+                                  const T* u_d, const T* v_d, const T* re_d, const T* im_d, const T* w_d,
+                                  double* chi2_d, cudaStream_t s) {
+        check_square(nx, ny);
+        check_nd(nd);
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        if (!s) s = c.stream;
+        DevState* st = as<DevState>(c.state, 1);
+        CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
+        Pipe<T>::enqueue(c, s, nx, (double)duv, img_d, nullptr, 0, 0, 0, 0, 0, nullptr, (double)v_origin, dRA, dDec,
+                         PA, nd, u_d, v_d, re_d, im_d, w_d, nullptr, true, chi2_d, st, false);
+    }
+
+    // ---- expert stages -------------------------------------------------
+    static void sweep(int nr, const T* I, T Rmin, T dR, int nxy, T dxy, T inc, T* image_padded) {
+        check_input(nxy);
+        reject_big(nxy);
+        ProfileGeom pg = profile_geom<T>(I, nr, Rmin, dR, dxy, nxy);
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        cudaStream_t s = c.stream;
+        const size_t nreal = (size_t)nxy * 2 * (size_t)(nxy / 2 + 1);
+        T* buf = as<T>(c.img, nreal);
+        T* I_d = as<T>(c.prof, (size_t)nr);
+        h2d(I_d, I, sizeof(T) * (size_t)nr, s);
+        CK(cudaMemsetAsync(buf, 0, sizeof(T) * nreal, s));
+        CK(L::sweep_image(I_d, nr, Rmin, dR, dxy, std::cos((double)inc), pg.rmax, pg.central, nxy, buf, s));
+        d2h(image_padded, buf, sizeof(T) * nreal, s);
+        CK(cudaStreamSynchronize(s));
+    }
+
+    static void uv_rotate(T PA, T dRA, T dDec, T* dRArot, T* dDecrot, int nd, const T* u, const T* v, T* urot,
+                          T* vrot) {
+        check_nd(nd);
+        if (PA == 0) {  // reference :1294-1299
+            *dRArot = dRA;
+            *dDecrot = dDec;
+            if (nd) {
+                std::memmove(urot, u, sizeof(T) * (size_t)nd);
+                std::memmove(vrot, v, sizeof(T) * (size_t)nd);
+            }
+            return;
+        }
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        cudaStream_t s = c.stream;
+        const double cs = std::cos((double)PA), sn = std::sin((double)PA);
+        T* u_d = as<T>(c.u, (size_t)nd);
+        T* v_d = as<T>(c.v, (size_t)nd);
+        T* ur_d = as<T>(c.urot, (size_t)nd);
+        T* vr_d = as<T>(c.vrot, (size_t)nd);
+        h2d(u_d, u, sizeof(T) * (size_t)nd, s);
+        h2d(v_d, v, sizeof(T) * (size_t)nd, s);
+        CK(L::rotate(u_d, v_d, ur_d, vr_d, nd, cs, sn, s));
+        d2h(urot, ur_d, sizeof(T) * (size_t)nd, s);
+        d2h(vrot, vr_d, sizeof(T) * (size_t)nd, s);
+        CK(cudaStreamSynchronize(s));
+        *dRArot = (T)((double)dRA * cs - (double)dDec * sn);
+        *dDecrot = (T)((double)dRA * sn + (double)dDec * cs);
+    }
+
+    static void interpolate(int nrow, int ncol, const T* data, T v_origin, int nd, const T* u, const T* v, T duv,
+                            T* vis) {
+        check_nd(nd);
+        if (nrow < 2 || ncol < 2) throw InvalidArg("Error in interpolate: the spectrum must be at least 2 x 2");
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        cudaStream_t s = c.stream;
+        CT* spec = as<CT>(c.win, (size_t)nrow * ncol);
+        T* u_d = as<T>(c.u, (size_t)nd);
+        T* v_d = as<T>(c.v, (size_t)nd);
+        CT* vis_d = as<CT>(c.vis, (size_t)nd);
+        DevState* st = as<DevState>(c.state, 1);
+        h2d(spec, data, sizeof(CT) * (size_t)nrow * ncol, s);
+        h2d(u_d, u, sizeof(T) * (size_t)nd, s);
+        h2d(v_d, v, sizeof(T) * (size_t)nd, s);
+        CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
+        typename L::VisArgs a;
+        a.spec = spec;
+        a.s_row = ncol;
+        a.s_col = 1;
+        a.nrow = nrow;
+        a.ncol = ncol;
+        a.host_K = ncol;
+        a.host_r0 = 0;
+        a.host_W = nrow;
+        a.duv = (double)duv;
+        a.v_origin = (double)v_origin;
+        a.rotate = false;
+        a.cos_pa = 1.;
+        a.sin_pa = 0.;
+        a.dra = a.ddec = 0.;
+        a.phase = false;
+        a.u = u_d;
+        a.v = v_d;
+        a.re = a.im = a.w = nullptr;
+        a.nd = nd;
+        a.vis_out = vis_d;
+        a.partials = nullptr;
+        a.chi2_out = nullptr;
+        a.state = st;
+        if (nd > 0) CK(L::vis(a, s));
+        d2h(vis, vis_d, sizeof(CT) * (size_t)nd, s);
+        finish(c, st);
+    }
+
+    static void apply_phase(T dRA, T dDec, int nd, const T* u, const T* v, T* vis) {
+        check_nd(nd);
+        if (dRA == 0 && dDec == 0) return;  // reference :890-892
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        cudaStream_t s = c.stream;
+        T* u_d = as<T>(c.u, (size_t)nd);
+        T* v_d = as<T>(c.v, (size_t)nd);
+        CT* vis_d = as<CT>(c.vis, (size_t)nd);
+        h2d(u_d, u, sizeof(T) * (size_t)nd, s);
+        h2d(v_d, v, sizeof(T) * (size_t)nd, s);
+        h2d(vis_d, vis, sizeof(CT) * (size_t)nd, s);
+        CK(L::apply_phase(u_d, v_d, vis_d, nd, (double)dRA, (double)dDec, s));
+        d2h(vis, vis_d, sizeof(CT) * (size_t)nd, s);
+        CK(cudaStreamSynchronize(s));
+    }
+
+    static void reduce_chi2(int nd, const T* re, const T* im, const T* vis, const T* w, T* chi2) {
+        check_nd(nd);
+        if (nd == 0) {
+            *chi2 = 0;
+            return;
+        }
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        cudaStream_t s = c.stream;
+        T* re_d = as<T>(c.re, (size_t)nd);
+        T* im_d = as<T>(c.im, (size_t)nd);
+        T* w_d = as<T>(c.w, (size_t)nd);
+        CT* vis_d = as<CT>(c.vis, (size_t)nd);
+        double* partials = as<double>(c.partials, (size_t)L::vis_grid(nd));
+        DevState* st = as<DevState>(c.state, 1);
+        h2d(re_d, re, sizeof(T) * (size_t)nd, s);
+        h2d(im_d, im, sizeof(T) * (size_t)nd, s);
+        h2d(w_d, w, sizeof(T) * (size_t)nd, s);
+        h2d(vis_d, vis, sizeof(CT) * (size_t)nd, s);
+        CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
+        CK(L::reduce(re_d, im_d, vis_d, w_d, nd, partials, st, s));
+        finish(c, st);
+        *chi2 = (T)c.host_state->chi2;
+    }
+
+    // in-place R2C of the padded layout (reference fft2d :531-541, _copy_input :460-487)
+    static void fft2d(int nx, int ny, T* data) {
+        check_square(nx, ny);
+        reject_big(nx);
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        cudaStream_t s = c.stream;
+        const int N = nx, C = N / 2 + 1;
+        T* img_d = as<T>(c.img, (size_t)N * N);
+        CT* zt = as<CT>(c.zt, (size_t)C * N);
+        CT* out = as<CT>(c.win, (size_t)C * N);
+        DevState* st = as<DevState>(c.state, 1);
+        CK(cudaMemcpy2DAsync(img_d, sizeof(T) * N, data, sizeof(T) * 2 * C, sizeof(T) * N, N, cudaMemcpyHostToDevice,
+                             s));
+        const CT* tw = c.twiddles<T>(N);
+        CK(L::rows_image(img_d, N, tw, zt, C, st, 1.0, false, s));
+        CK(L::cols(zt, N, 0, N, tw, out, C, 1, C, 0, N, st, 1.0, false, s));
+        d2h(data, out, sizeof(CT) * (size_t)N * C, s);
+        CK(cudaStreamSynchronize(s));
+    }
+
+    static void fftshift(int nx, int ny, T* data) {
+        check_square(nx, ny);
+        reject_big(nx);
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        cudaStream_t s = c.stream;
+        const size_t nreal = (size_t)nx * 2 * (size_t)(ny / 2 + 1);
+        T* buf = as<T>(c.img, nreal);
+        h2d(buf, data, sizeof(T) * nreal, s);
+        CK(L::fftshift_real(buf, nx, s));
+        d2h(data, buf, sizeof(T) * nreal, s);
+        CK(cudaStreamSynchronize(s));
+    }
+
+    static void fftshift_axis0(int nrow, int ncol, T* data) {
+        check_input(nrow);
+        Ctx& c = ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        cudaStream_t s = c.stream;
+        const size_t n = (size_t)nrow * ncol;
+        CT* buf = as<CT>(c.win, n);
+        h2d(buf, data, sizeof(CT) * n, s);
+        CK(L::fftshift_axis0(buf, nrow, ncol, s));
+        d2h(data, buf, sizeof(CT) * n, s);
+        CK(cudaStreamSynchronize(s));
+    }
+};
+
+}  // namespace
+}  // namespace gbg
+
+using gbg::Api;
+using gbg::guarded;
+
+#define API extern "C" __attribute__((visibility("default")))
+
+API const char* galario_last_error(void) { return gbg::g_msg.c_str(); }
+API const char* galario_version(void) { return "galario_gb300 0.1.0 (reference API galario 1.2.2)"; }
+
+API int galario_threads(int num) {
+    if (num > 0) gbg::g_tpb = num;
+    return gbg::g_tpb;
+}
+API int galario_ngpus(int* out) {
+    return guarded([&] {
+        int n = 0;
+        gbg::cuda_check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+        *out = n;
+    });
+}
+API int galario_use_gpu(int device_id) {
+    return guarded([&] { gbg::cuda_check(cudaSetDevice(device_id), "cudaSetDevice"); });
+}
+API int galario_init(void) {
+    return guarded([&] { (void)gbg::ctx(); });
+}
+API int galario_cleanup(void) {
+    return guarded([&] {
+        std::lock_guard<std::mutex> lk(gbg::g_ctx_mu);
+        for (auto& kv : gbg::g_ctx) {
+            std::lock_guard<std::mutex> l2(kv.second->mu);
+            int cur = 0;
+            cudaGetDevice(&cur);
+            cudaSetDevice(kv.first);
+            cudaStreamSynchronize(kv.second->stream);
+            kv.second->release_all();
+            cudaSetDevice(cur);
+        }
+    });
+}
+
+// precision-specific entry points, generated for double (_d) and float (_f)
+#define GALARIO_DEFINE(R, SFX)                                                                                        \
+    API int galario_sample_image##SFX(int nx, int ny, const R* image, R v_origin, R dRA, R dDec, R duv, R PA, int nd, \
+                                      const R* u, const R* v, R* vis) {                                               \
+        return guarded([&] { Api<R>::sample_image(nx, ny, image, v_origin, dRA, dDec, duv, PA, nd, u, v, vis); });   \
+    }                                                                                                                 \
+    API int galario_chi2_image##SFX(int nx, int ny, const R* image, R v_origin, R dRA, R dDec, R duv, R PA, int nd,   \
+                                    const R* u, const R* v, const R* re, const R* im, const R* w, R* chi2) {          \
+        return guarded(                                                                                               \
+            [&] { Api<R>::chi2_image(nx, ny, image, v_origin, dRA, dDec, duv, PA, nd, u, v, re, im, w, chi2); });     \
+    }                                                                                                                 \
+    API int galario_sample_profile##SFX(int nr, const R* intensity, R Rmin, R dR, R dxy, int nxy, R inc, R dRA,       \
+                                        R dDec, R duv, R PA, int nd, const R* u, const R* v, R* vis) {                \
+        return guarded([&] {                                                                                          \
+            Api<R>::sample_profile(nr, intensity, Rmin, dR, dxy, nxy, inc, dRA, dDec, duv, PA, nd, u, v, vis);        \
+        });                                                                                                           \
+    }                                                                                                                 \
+    API int galario_chi2_profile##SFX(int nr, const R* intensity, R Rmin, R dR, R dxy, int nxy, R inc, R dRA, R dDec, \
+                                      R duv, R PA, int nd, const R* u, const R* v, const R* re, const R* im,          \
+                                      const R* w, R* chi2) {                                                          \
+        return guarded([&] {                                                                                          \
+            Api<R>::chi2_profile(nr, intensity, Rmin, dR, dxy, nxy, inc, dRA, dDec, duv, PA, nd, u, v, re, im, w,     \
+                                 chi2);                                                                               \
+        });                                                                                                           \
+    }                                                                                                                 \
+    API int galario_chi2_profile_device##SFX(int nr, const R* intensity_host, const R* intensity_dev, R Rmin, R dR,   \
+                                             R dxy, int nxy, R inc, R dRA, R dDec, R duv, R PA, int nd,               \
+                                             const R* u_dev, const R* v_dev, const R* re_dev, const R* im_dev,        \
+                                             const R* w_dev, double* chi2_dev, void* stream) {                        \
+        return guarded([&] {                                                                                          \
+            Api<R>::chi2_profile_device(nr, intensity_host, intensity_dev, Rmin, dR, dxy, nxy, inc, dRA, dDec, duv,   \
+                                        PA, nd, u_dev, v_dev, re_dev, im_dev, w_dev, chi2_dev,                        \
+                                        static_cast<cudaStream_t>(stream));                                          \
+        });                                                                                                           \
+    }                                                                                                                 \
+    API int galario_chi2_image_device##SFX(int nx, int ny, const R* image_dev, R v_origin, R dRA, R dDec, R duv,      \
+                                           R PA, int nd, const R* u_dev, const R* v_dev, const R* re_dev,             \
+                                           const R* im_dev, const R* w_dev, double* chi2_dev, void* stream) {         \
+        return guarded([&] {                                                                                          \
+            Api<R>::chi2_image_device(nx, ny, image_dev, v_origin, dRA, dDec, duv, PA, nd, u_dev, v_dev, re_dev,      \
+                                      im_dev, w_dev, chi2_dev, static_cast<cudaStream_t>(stream));                    \
+        });                                                                                                           \
+    }                                                                                                                 \
+    API int galario_sweep##SFX(int nr, const R* intensity, R Rmin, R dR, int nxy, R dxy, R inc, R* image) {           \
+        return guarded([&] { Api<R>::sweep(nr, intensity, Rmin, dR, nxy, dxy, inc, image); });                       \
+    }                                                                                                                 \
+    API int galario_uv_rotate##SFX(R PA, R dRA, R dDec, R* dRArot, R* dDecrot, int nd, const R* u, const R* v,        \
+                                   R* urot, R* vrot) {                                                                \
+        return guarded([&] { Api<R>::uv_rotate(PA, dRA, dDec, dRArot, dDecrot, nd, u, v, urot, vrot); });            \
+    }                                                                                                                 \
+    API int galario_interpolate##SFX(int nrow, int ncol, const R* data, R v_origin, int nd, const R* u, const R* v,   \
+                                     R duv, R* vis) {                                                                 \
+        return guarded([&] { Api<R>::interpolate(nrow, ncol, data, v_origin, nd, u, v, duv, vis); });                \
+    }                                                                                                                 \
+    API int galario_apply_phase_sampled##SFX(R dRA, R dDec, int nd, const R* u, const R* v, R* vis) {                \
+        return guarded([&] { Api<R>::apply_phase(dRA, dDec, nd, u, v, vis); });                                      \
+    }                                                                                                                 \
+    API int galario_reduce_chi2##SFX(int nd, const R* re, const R* im, const R* vis, const R* w, R* chi2) {           \
+        return guarded([&] { Api<R>::reduce_chi2(nd, re, im, vis, w, chi2); });                                      \
+    }                                                                                                                 \
+    API int galario_fft2d##SFX(int nx, int ny, R* data) {                                                             \
+        return guarded([&] { Api<R>::fft2d(nx, ny, data); });                                                        \
+    }                                                                                                                 \
+    API int galario_fftshift##SFX(int nx, int ny, R* data) {                                                          \
+        return guarded([&] { Api<R>::fftshift(nx, ny, data); });                                                     \
+    }                                                                                                                 \
+    API int galario_fftshift_axis0##SFX(int nrow, int ncol, R* data) {                                                \
+        return guarded([&] { Api<R>::fftshift_axis0(nrow, ncol, data); });                                           \
+    }
+
+GALARIO_DEFINE(double, _d)
+GALARIO_DEFINE(float, _f)
+
+API int galario_device_status(unsigned int* err_bits) {
+    return guarded([&] {
+        gbg::Ctx& c = gbg::ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        gbg::DevState* st = gbg::as<gbg::DevState>(c.state, 1);
+        gbg::d2h(c.host_state, st, sizeof(gbg::DevState), c.stream);
+        gbg::cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+        *err_bits = c.host_state->err;
+    });
+}

@@ -1,0 +1,127 @@
+// Internal declarations shared by the galario_gb300 CUDA translation units.
+//
+// Data layout in HBM for one model evaluation (N = nxy, C = N/2 + 1):
+//   image     N x N real, row-major (sampleImage/chi2Image input)        [optional]
+//   zt        K x N complex, column-major ("transposed rows"): zt[k*N + i] is
+//             the k-th real-FFT output of image row i times (-1)^i
+//   window    K x W complex, column-major: window[k*W + (r - r0)] is the
+//             fftshift-ed half-plane spectrum S[r][k] for rows r in [r0, r0+W)
+//   u, v, re, im, w   nd reals each (structure of arrays)
+// K (columns) and [r0, r0+W) (rows) are the part of the spectrum the uv
+// points can touch; they follow from max(u^2+v^2) and are computed on the
+// device by window_from_extent() so that no host round trip is needed.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbg {
+
+template <typename T> struct Cplx;
+template <> struct Cplx<double> { using type = double2; };
+template <> struct Cplx<float> { using type = float2; };
+template <typename T> using C2 = typename Cplx<T>::type;
+
+// Device-side state of one pipeline run (lives in device memory, 64 bytes).
+struct DevState {
+    double rmax2;                 // max(u^2 + v^2) over the dataset (atomicMax on the bit pattern)
+    double chi2;                  // final chi2 (written by the last reduction block)
+    unsigned int err;             // error bits, see ERR_*
+    unsigned int ticket;          // last-block-done counter of the chi2 reduction
+    unsigned long long err_index; // first offending visibility index (best effort)
+    double pad[4];
+};
+
+enum : unsigned int {
+    ERR_UV_OUTSIDE = 1u,     // a bilinear corner falls outside the N x (N/2+1) spectrum
+    ERR_UV_NONFINITE = 2u,   // u or v is NaN/inf
+    ERR_WINDOW = 4u,         // internal: corner outside the computed window (should not happen)
+    ERR_SPIN = 8u,           // a bounded wait gave up
+};
+
+// The part of the half-plane spectrum that can be touched by uv points whose
+// radius is at most sqrt(rmax2):  columns [0, K), rows [r0, r0 + W).
+struct Window {
+    int K, r0, W;
+};
+
+__host__ __device__ inline Window window_from_extent(double rmax2, double duv, int N) {
+    const int C = N / 2 + 1;
+    Window w;
+    double ext = sqrt(rmax2) / duv;
+    ext = ext * (1.0 + 1e-9) + 1e-9;           // rotation/rounding margin
+    if (!(ext < 4.0 * N)) ext = 4.0 * N;       // NaN/inf/huge: clamp (points get flagged later)
+    int fu = (int)floor(ext);
+    int K = fu + 2;                             // fl_u and fl_u + 1
+    if (K > C) K = C;
+    int kv = (int)ceil(ext);
+    int r0 = N / 2 - kv - 1;
+    int r1 = N / 2 + kv + 3;                    // fl_v + 1, and fl_v + 2 for the row wrap at u column C-1
+    if (r0 < 0) r0 = 0;
+    if (r1 > N) r1 = N;
+    w.K = K;
+    w.r0 = r0;
+    w.W = r1 - r0;
+    return w;
+}
+
+inline bool is_pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// ---------------------------------------------------------------------------
+// Kernel launchers (gb_kernels.cu).  All are asynchronous on `stream`.
+// ---------------------------------------------------------------------------
+template <typename T> struct Launch {
+    using CT = C2<T>;
+    // dataset extent: state->rmax2 = max(u^2 + v^2)
+    static cudaError_t extent(const T* u, const T* v, int nd, DevState* state, cudaStream_t s);
+    // row pass on an image (rows [0, N)), output zt for columns [0, K) where
+    // K = host_K if >= 0, else from state->rmax2 (window_from_extent).
+    // row_sign: multiply row i by (-1)^i.
+    static cudaError_t rows_image(const T* image, int N, const CT* tw, CT* zt, int host_K, const DevState* state,
+                                  double duv, bool row_sign, cudaStream_t s);
+    // row pass fused with the profile sweep: only rows [N/2 - rmax, N/2 + rmax) are nonzero
+    static cudaError_t rows_profile(const T* intensity, int nr, double Rmin, double dR, double dxy, double cos_inc,
+                                    int rmax, double central_value, int N, const CT* tw, CT* zt, const DevState* state,
+                                    double duv, cudaStream_t s);
+    // column pass: column FFTs of zt (rows outside [band0, band1) are zero) and
+    // write rows [r0, r0+W) of columns [0, K) to out[(r - r0)*s_row + k*s_col],
+    // times (-1)^(r + k + N/2) if out_sign.  host_K/host_r0/host_W >= 0 override
+    // the device-derived window.
+    static cudaError_t cols(const CT* zt, int N, int band0, int band1, const CT* tw, CT* out, long long s_row,
+                            long long s_col, int host_K, int host_r0, int host_W, const DevState* state, double duv,
+                            bool out_sign, cudaStream_t s);
+    // fused rotation + interpolation + phase + (vis out) + (chi2 reduction)
+    struct VisArgs {
+        const CT* spec;      // spectrum window
+        long long s_row, s_col;
+        int nrow, ncol;      // logical N and C of the full spectrum (flat-index semantics)
+        int host_K, host_r0, host_W;  // window (>= 0) or derive from state
+        double duv, v_origin, cos_pa, sin_pa;
+        bool rotate;         // PA != 0
+        double dra, ddec;    // rotated offsets (radians, not yet times 2 pi)
+        bool phase;          // dra != 0 || ddec != 0
+        const T *u, *v, *re, *im, *w;
+        int nd;
+        CT* vis_out;         // may be null
+        double* partials;    // chi2 partials (null: no chi2)
+        double* chi2_out;    // optional extra copy of the final chi2 (device)
+        DevState* state;
+    };
+    static cudaError_t vis(const VisArgs& a, cudaStream_t s);
+    static int vis_grid(int nd);
+    // expert-stage kernels
+    static cudaError_t fftshift_real(T* padded, int N, cudaStream_t s);
+    static cudaError_t fftshift_axis0(CT* m, int nrow, int ncol, cudaStream_t s);
+    static cudaError_t apply_phase(const T* u, const T* v, CT* vis, int nd, double dra, double ddec, cudaStream_t s);
+    static cudaError_t rotate(const T* u, const T* v, T* urot, T* vrot, int nd, double c, double sn, cudaStream_t s);
+    static cudaError_t reduce(const T* re, const T* im, const CT* vis, const T* w, int nd, double* partials,
+                              DevState* state, cudaStream_t s);
+    static cudaError_t sweep_image(const T* intensity, int nr, double Rmin, double dR, double dxy, double cos_inc,
+                                   int rmax, double central_value, int N, T* padded, cudaStream_t s);
+    // largest N the shared-memory FFT kernels handle for this precision
+    static int max_fft_n();
+};
+
+int num_sms();
+
+}  // namespace gbg
