@@ -1,0 +1,430 @@
+#!/usr/bin/env python
+"""Benchmark: chi2 evaluations per second of galario's chi2Profile on the
+nxy=4096, 2M-visibility workload (double-ring profile, inc 40 deg, PA 70 deg).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one chi2Profile evaluation of one model over all 2M visibilities.
+Prints ONE JSON line (rank 0).  Under torchrun (N > 1) every rank evaluates
+its own replica of the workload (the path has no data exchange), the time is
+the max over ranks and `value` counts the evaluations of all ranks.
+
+--impl ours (default)
+  value        device-resident plain FP64 chi2Profile (galario_gb300 C ABI,
+               inputs already in HBM, L2 flushed between steps, the flush
+               outside the CUDA-event-timed region)
+  e2e          the same through the public Python API (galario_gb300.double.
+               chi2Profile) with inputs in pinned host memory: every step copies
+               intensity, u, v, Re, Im, w to the device and reads chi2 back
+  single       the same for the FP32 module (galario_gb300.single)
+  roofline     dominant kernel: algorithmic bytes / mean CUDA-event duration
+  cpu_baseline the CPU oracle (C restatement of the reference CPU path) timed
+               on a bounded sample on this host's cores
+--impl reference
+  the reference's CPU implementation of the path (the reference build in
+  oracle/_ref when present, else the C restatement oracle/_build), on all
+  host cores, same workload, same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("chi2 evals/s, nxy=4096, 2M vis: plain FP64 vs batched FP32+grad, ≤1e-6 rel chi2")
+UNIT = "evals/s"
+ARCSEC = 4.84813681109536e-06
+DEG = 0.017453292519943295
+
+
+# ---------------------------------------------------------------------------
+# workload: nxy=4096, dxy=3e-3", double-ring profile (r0 0.2"/0.6", sigma
+# 0.03"/0.08", amplitudes 1:0.4, total flux 0.1 Jy), Rmin=1e-4", dR=2.5e-4"
+# (the reference's central-pixel check rejects dR=1e-3" at this dxy),
+# nr=4096, inc=40 deg, PA=70 deg, dRA/dDec ~ U[-0.05, 0.05]", Nvis=2e6 with
+# radius log-uniform in [1e4, 4e6] wavelengths and uniform angle; noise
+# sigma ~ U[0.5, 1.5] mJy on Re and Im, w = 1/sigma^2; seed 0.  Synthetic.
+# ---------------------------------------------------------------------------
+class Workload:
+    nxy = 4096
+    dxy = 3e-3 * ARCSEC
+    nr = 4096
+    Rmin = 1e-4 * ARCSEC
+    dR = 2.5e-4 * ARCSEC
+    inc = 40 * DEG
+    PA = 70 * DEG
+    nd = 2_000_000
+
+    def __init__(self, seed=0):
+        rng = np.random.default_rng(seed)
+        R = self.Rmin + self.dR * np.arange(self.nr)
+        ring = (np.exp(-0.5 * ((R - 0.2 * ARCSEC) / (0.03 * ARCSEC)) ** 2) +
+                0.4 * np.exp(-0.5 * ((R - 0.6 * ARCSEC) / (0.08 * ARCSEC)) ** 2))
+        trap = getattr(np, "trapezoid", None) or np.trapz
+        flux = trap(ring * 2 * np.pi * R, R)
+        self.intensity_scale = 0.1 / flux          # Jy/sr per unit profile
+        self.intensity = ring * self.intensity_scale
+        self.dRA, self.dDec = rng.uniform(-0.05, 0.05, 2) * ARCSEC
+        r = np.exp(rng.uniform(np.log(1e4), np.log(4e6), self.nd))
+        th = rng.uniform(0, 2 * np.pi, self.nd)
+        self.u, self.v = r * np.cos(th), r * np.sin(th)
+        self.sigma = rng.uniform(0.5e-3, 1.5e-3, self.nd)
+        self.noise_re = rng.normal(0, self.sigma)
+        self.noise_im = rng.normal(0, self.sigma)
+        self.w = 1. / self.sigma ** 2
+
+    @property
+    def duv(self):
+        return 1. / (self.dxy * self.nxy)
+
+    def kw(self):
+        return dict(dRA=float(self.dRA), dDec=float(self.dDec), PA=self.PA, inc=self.inc)
+
+    def args(self):
+        return (self.intensity, self.Rmin, self.dR, self.nxy, self.dxy)
+
+    def config(self):
+        return {"workload": "chi2Profile nxy=4096 dxy=3e-3\" Nvis=2e6 double-ring nr=4096 dR=2.5e-4\" "
+                            "inc=40deg PA=70deg (config 1)",
+                "nxy": self.nxy, "nvis": self.nd, "nr": self.nr, "global_batch": 1,
+                "parallelism": "replicas", "l2": "flushed between steps (256 MiB write, outside the timed events)"}
+
+    def window(self):
+        """The part of the spectrum the kernels touch (same rule as the library)."""
+        N = self.nxy
+        ext = np.sqrt(np.max(self.u ** 2 + self.v ** 2)) / self.duv * (1 + 2e-6) + 1e-6
+        K = min(N // 2 + 1, int(np.floor(ext)) + 2)
+        kv = int(np.ceil(ext))
+        r0, r1 = max(0, N // 2 - kv - 1), min(N, N // 2 + kv + 3)
+        rmax = min(int(np.ceil((self.Rmin + self.nr * self.dR) / self.dxy)), N // 2)
+        return K, r1 - r0, 2 * rmax
+
+
+def algorithmic_bytes(wl: Workload, s: int):
+    """Algorithmic HBM bytes per launch of each stage, s = bytes per real."""
+    K, W, R = wl.window()
+    N, nd = wl.nxy, wl.nd
+    return {
+        "extent": nd * 2 * s,                                  # read u, v
+        "rows": R * K * 2 * s + wl.nr * s,                     # sweep fused: write R x K complex, read profile
+        "cols": K * R * 2 * s + K * W * 2 * s,                 # read band rows, write window rows
+        "vis": nd * 5 * s,                                     # read u, v, Re, Im, w (gathers hit L2)
+        "quad": K * W * 3 * s + K * W * 16 * s,                # read window + moduli, write cell records
+    }, {"K": K, "W": W, "R_rows": R}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        if not getattr(self, "out", ""):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for row in csv.reader(io.StringIO(self.out)):
+            if len(row) < 9:
+                continue
+            try:
+                sm.append(float(row[1]))
+                mx.append(float(row[2]))
+            except ValueError:
+                continue
+            for n, val in zip(names, row[5:9]):
+                if val.strip().lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle) -- only here and in --impl reference
+# ---------------------------------------------------------------------------
+def cpu_chi2_profile_rate(wl: Workload, re, im, steps: int, prefer_ref: bool = True):
+    from oracle import oracle as O
+    kind = "port"
+    if prefer_ref and O.have_ref():
+        impl, kind = O.get("ref", "double"), "reference"
+    else:
+        O.build_port()
+        impl = O.get("port", "double")
+    cores = len(os.sched_getaffinity(0))
+    impl.threads(cores)
+    args = wl.args()
+    impl.chi2Profile(*args, wl.u, wl.v, re, im, wl.w, **wl.kw())  # first call dropped (speed_benchmark.py:170-172)
+    t0 = time.perf_counter()
+    chi2 = None
+    for _ in range(steps):
+        chi2 = impl.chi2Profile(*args, wl.u, wl.v, re, im, wl.w, **wl.kw())
+    dt = time.perf_counter() - t0
+    return steps / dt, kind, cores, chi2, dt
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    wl = Workload()
+    from oracle import oracle as O
+    if not O.have_ref():
+        O.build_port()
+    impl = O.get("ref", "double") if O.have_ref() else O.get("port", "double")
+    impl.threads(len(os.sched_getaffinity(0)))
+    model = impl.sampleProfile(*wl.args(), wl.u, wl.v, **wl.kw())
+    re, im = model.real + wl.noise_re, model.imag + wl.noise_im
+    for _ in range(max(args.warmup, 1)):
+        impl.chi2Profile(*wl.args(), wl.u, wl.v, re, im, wl.w, **wl.kw())
+    rate, kind, cores, chi2, dt = cpu_chi2_profile_rate(wl, re, im, args.steps)
+    line = {"metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": wl.config(),
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": "%d full chi2Profile evaluations (galario.double CPU path, FFT from the "
+                                       "project's C FFT in place of FFTW)" % args.steps},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "chi2": chi2}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import ctypes as C
+
+    import torch
+
+    import galario_gb300 as g
+    from galario_gb300 import _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    g.double.use_gpu(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    wl = Workload(seed=0)
+    L = _lib.lib()
+    dev = torch.device("cuda", local)
+    # a dedicated stream: the library's kernels, the L2 flush and the timing
+    # events are all ordered on it
+    stream = torch.cuda.Stream(dev)
+    sptr = C.c_void_p(stream.cuda_stream)
+
+    # observations: model from the product itself plus noise
+    model = g.double.sampleProfile(*wl.args(), wl.u, wl.v, **wl.kw())
+    re = model.real + wl.noise_re
+    im = model.imag + wl.noise_im
+
+    def to_dev(a, dt):
+        return torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def device_rate(precision):
+        dt = torch.float64 if precision == "double" else torch.float32
+        R = C.c_double if precision == "double" else C.c_float
+        npdt = np.float64 if precision == "double" else np.float32
+        I_host = np.ascontiguousarray(wl.intensity, dtype=npdt)
+        I_d = to_dev(wl.intensity, dt)
+        u_d, v_d, re_d, im_d, w_d = (to_dev(x, dt) for x in (wl.u, wl.v, re, im, wl.w))
+        chi2_d = torch.zeros(1, dtype=torch.float64, device=dev)
+        fn = _lib.fn("chi2_profile_device", precision)
+        kw = wl.kw()
+        cargs = (wl.nr, I_host.ctypes.data, I_d.data_ptr(), R(wl.Rmin), R(wl.dR), R(wl.dxy), wl.nxy, R(kw["inc"]),
+                 R(kw["dRA"]), R(kw["dDec"]), R(wl.duv), R(kw["PA"]), wl.nd, u_d.data_ptr(), v_d.data_ptr(),
+                 re_d.data_ptr(), im_d.data_ptr(), w_d.data_ptr(), chi2_d.data_ptr(), sptr)
+
+        def step():
+            _lib.check(fn(*cargs))
+
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                flush.zero_()
+                step()
+        torch.cuda.synchronize()
+        _lib.check(L.galario_stage_timing(1))
+        _lib.check(L.galario_stage_times((C.c_double * 8)(), (C.c_int * 8)(), 8))  # discard warm-up records
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk, torch.cuda.stream(stream):
+            t0 = time.perf_counter()
+            for a, b in evs:
+                flush.zero_()
+                a.record(stream)
+                step()
+                b.record(stream)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        if dist is not None:
+            dist.barrier()
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        ms_sum = (C.c_double * 8)()
+        cnt = (C.c_int * 8)()
+        _lib.check(L.galario_stage_times(ms_sum, cnt, 8))
+        _lib.check(L.galario_stage_timing(0))
+        err = C.c_uint(0)
+        _lib.check(L.galario_device_status(C.byref(err)))
+        if err.value:
+            raise RuntimeError("device error bits %d" % err.value)
+        stages = {L.galario_stage_name(i).decode(): (ms_sum[i] / cnt[i] if cnt[i] else 0.0) for i in range(8)
+                  if cnt[i]}
+        return ms, stages, float(chi2_d.item()), clk.summary(), wall
+
+    ms64, stages64, chi2_64, clocks, wall64 = device_rate("double")
+    ms32, stages32, chi2_32, _, _ = device_rate("single")
+
+    # max over ranks of the timed region
+    t_local = ms64 / 1e3
+    if dist is not None:
+        t = torch.tensor([t_local], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_local = float(t.item())
+    value = world * args.steps / t_local
+
+    # e2e: public API, pinned host inputs, H2D + D2H inside every step
+    def pinned(a, dt):
+        t = torch.empty(len(a), dtype=dt, pin_memory=True)
+        arr = t.numpy()
+        arr[:] = a
+        return t, arr
+
+    keep = []
+    host = {}
+    for name, a in (("I", wl.intensity), ("u", wl.u), ("v", wl.v), ("re", re), ("im", im), ("w", wl.w)):
+        t, arr = pinned(a, torch.float64)
+        keep.append(t)
+        host[name] = arr
+    e2e_chi2 = None
+    for _ in range(max(1, min(args.warmup, 3))):
+        e2e_chi2 = g.double.chi2Profile(host["I"], wl.Rmin, wl.dR, wl.nxy, wl.dxy, host["u"], host["v"], host["re"],
+                                        host["im"], host["w"], **wl.kw())
+    e2e_steps = args.steps
+    if dist is not None:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_chi2 = g.double.chi2Profile(host["I"], wl.Rmin, wl.dR, wl.nxy, wl.dxy, host["u"], host["v"],
+                                        host["re"], host["im"], host["w"], **wl.kw())
+    e2e_t = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_t], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_value = world * e2e_steps / e2e_t
+    h2d_bytes = 8 * (wl.nr + 5 * wl.nd)
+    d2h_bytes = 64  # device state block carrying chi2 and the error bits
+
+    line = None
+    if rank == 0:
+        hbm, peak_kind = peaks()
+        alg, win = algorithmic_bytes(wl, 8)
+        dom = max((k for k in stages64 if k in alg), key=lambda k: stages64[k])
+        achieved = alg[dom] / (stages64[dom] * 1e-3) / 1e9
+        rate_cpu, kind, cores, chi2_cpu, dt_cpu = cpu_chi2_profile_rate(wl, re, im, steps=2)
+        alg32, _ = algorithmic_bytes(wl, 4)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms64 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": wl.config(),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes,
+                    "d2h_bytes_per_step": d2h_bytes, "api": "galario_gb300.double.chi2Profile, pinned numpy inputs"},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                         "traffic": None, "algorithmic_bytes": alg[dom],
+                         "note": "FP64 arithmetic on GB300 runs at ~1.2 TFLOP/s; the FP64 kernels are "
+                                 "FP64-issue-bound, not HBM-bound"},
+            "stages_ms": {k: round(v, 4) for k, v in stages64.items()},
+            "window": win,
+            "single": {"value": world * args.steps / (ms32 / 1e3), "unit": UNIT, "dtype": "f32",
+                       "ms_per_step": ms32 / args.steps, "stages_ms": {k: round(v, 4) for k, v in stages32.items()},
+                       "rel_chi2_vs_f64": abs(chi2_32 - chi2_64) / abs(chi2_64),
+                       "vis_GBs": alg32["vis"] / (stages32.get("vis", 1e9) * 1e-3) / 1e9},
+            "cpu_baseline": {"value": rate_cpu, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": "2 full chi2Profile evaluations (FP64, FFT from the project's C FFT in place "
+                                       "of FFTW), first call dropped"},
+            "parity": {"chi2_f64": chi2_64, "chi2_e2e": e2e_chi2, "chi2_cpu": chi2_cpu,
+                       "rel_f64_vs_cpu": abs(chi2_64 - chi2_cpu) / abs(chi2_cpu)},
+            "gpu_launches": 5 * args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

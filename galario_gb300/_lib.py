@@ -71,7 +71,12 @@ def lib() -> C.CDLL:
         L.galario_init.argtypes = []
         L.galario_cleanup.argtypes = []
         L.galario_device_status.argtypes = [C.POINTER(C.c_uint)]
-        for n in ("galario_ngpus", "galario_use_gpu", "galario_init", "galario_cleanup", "galario_device_status"):
+        L.galario_stage_timing.argtypes = [_i]
+        L.galario_stage_name.argtypes = [_i]
+        L.galario_stage_name.restype = C.c_char_p
+        L.galario_stage_times.argtypes = [C.POINTER(C.c_double), C.POINTER(_i), _i]
+        for n in ("galario_ngpus", "galario_use_gpu", "galario_init", "galario_cleanup", "galario_device_status",
+                  "galario_stage_timing", "galario_stage_times"):
             getattr(L, n).restype = _i
         _lib = L
         return L

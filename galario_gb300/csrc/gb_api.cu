@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -110,17 +111,46 @@ struct Ctx {
     int device = 0;
     std::mutex mu;
     cudaStream_t stream = nullptr;
-    DevBuf state, partials, img, prof, u, v, re, im, w, vis, zt, win, urot, vrot;
+    DevBuf state, partials, img, prof, u, v, re, im, w, vis, zt, win, amp, quad, urot, vrot;
+    double2* phase_tab = nullptr;  // table of the FP64 phase shift (PHASE_T + 1 entries)
     std::map<std::pair<int, int>, void*> tw;  // (N, sizeof(T)) -> table
     DevState* host_state = nullptr;           // pinned mirror of DevState
+    // optional per-stage CUDA-event timing (galario_stage_timing)
+    bool timing = false;
+    struct Rec {
+        int stage;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> spare;
+    cudaEvent_t event() {
+        cudaEvent_t e;
+        if (!spare.empty()) {
+            e = spare.back();
+            spare.pop_back();
+            return e;
+        }
+        CK(cudaEventCreate(&e));
+        return e;
+    }
 
     void init(int dev) {
         device = dev;
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         CK(cudaMallocHost(&host_state, sizeof(DevState)));
+        // exp(2 pi i (j - T/2) / T), j in [0, T], evaluated in long double
+        std::vector<double2> h(PHASE_T + 1);
+        const long double two_pi = 6.283185307179586476925286766559005768L;
+        for (int j = 0; j <= PHASE_T; ++j) {
+            long double a = two_pi * (long double)(j - PHASE_T / 2) / (long double)PHASE_T;
+            h[(size_t)j] = make_double2((double)cosl(a), (double)sinl(a));
+        }
+        CK(cudaMalloc(&phase_tab, sizeof(double2) * (PHASE_T + 1)));
+        CK(cudaMemcpy(phase_tab, h.data(), sizeof(double2) * (PHASE_T + 1), cudaMemcpyHostToDevice));
     }
     void release_all() {
-        DevBuf* bufs[] = {&state, &partials, &img, &prof, &u, &v, &re, &im, &w, &vis, &zt, &win, &urot, &vrot};
+        DevBuf* bufs[] = {&state, &partials, &img, &prof, &u, &v, &re, &im, &w, &vis, &zt, &win, &amp, &quad,
+                          &urot, &vrot};
         for (DevBuf* b : bufs) b->release();
         for (auto& kv : tw) cudaFree(kv.second);
         tw.clear();
@@ -160,6 +190,21 @@ Ctx& ctx() {
     g_ctx[dev] = c;
     return *c;
 }
+
+// Run f (which enqueues work on s); with timing on, bracket it with events.
+template <class F> void timed(Ctx& c, cudaStream_t s, int stage, F&& f) {
+    if (!c.timing) {
+        f();
+        return;
+    }
+    cudaEvent_t a = c.event(), b = c.event();
+    CK(cudaEventRecord(a, s));
+    f();
+    CK(cudaEventRecord(b, s));
+    c.recs.push_back(Ctx::Rec{stage, a, b});
+}
+enum { ST_H2D = 0, ST_EXTENT, ST_ROWS, ST_COLS, ST_VIS, ST_D2H, ST_QUAD, ST_COUNT };
+const char* const kStageNames[ST_COUNT] = {"h2d", "extent", "rows", "cols", "vis", "d2h", "quad"};
 
 template <typename T> T* as(DevBuf& b, size_t count) { return static_cast<T*>(b.get(sizeof(T) * count)); }
 
@@ -224,6 +269,7 @@ template <typename T>
 ProfileGeom profile_geom(const T* I_host, int nr, double Rmin, double dR, double dxy, int nxy) {
     check_central_pixel(dxy, Rmin, dR);
     if (nr < 2) throw InvalidArg("Error in create image: the intensity profile needs at least 2 samples");
+    if (nr >= (1 << 22)) throw InvalidArg("Error in create image: the intensity profile is limited to 2^22 samples");
     std::vector<double> Id((size_t)nr);
     for (int i = 0; i < nr; ++i) Id[(size_t)i] = (double)I_host[i];
     ProfileGeom g;
@@ -251,20 +297,32 @@ template <typename T> struct Pipe {
         const CT* tw = c.twiddles<T>(N);
         CT* zt = as<CT>(c.zt, (size_t)C * N);
         CT* win = as<CT>(c.win, (size_t)C * N);
+        T* amp = as<T>(c.amp, (size_t)C * N);
+        const long long qcap = std::min<long long>((long long)C * N, QUAD_CAP);
+        T* quads = as<T>(c.quad, (size_t)qcap * QUAD_REC);
         double* partials = as<double>(c.partials, (size_t)L::vis_grid(nd > 0 ? nd : 1));
-        if (!have_extent) CK(L::extent(u, v, nd, st, s));
+        if (!have_extent) timed(c, s, ST_EXTENT, [&] { CK(L::extent(u, v, nd, N, duv, st, s)); });
         int band0 = 0, band1 = N;
         if (img) {
-            CK(L::rows_image(img, N, tw, zt, -1, st, duv, true, s));
+            timed(c, s, ST_ROWS, [&] { CK(L::rows_image(img, N, tw, zt, -1, st, duv, true, s)); });
         } else {
             band0 = N / 2 - pg->rmax;
             band1 = N / 2 + pg->rmax;
-            CK(L::rows_profile(prof, nr, Rmin, dR, dxy, std::cos(inc), pg->rmax, pg->central, N, tw, zt, st, duv, s));
+            timed(c, s, ST_ROWS, [&] {
+                CK(L::rows_profile(prof, nr, Rmin, dR, dxy, std::cos(inc), pg->rmax, pg->central, N, tw, zt, st,
+                                   duv, s));
+            });
         }
         // window layout: column k at win + k*N, rows [r0, r0+W) contiguous
-        CK(L::cols(zt, N, band0, band1, tw, win, 1, N, -1, -1, -1, st, duv, true, s));
+        timed(c, s, ST_COLS,
+              [&] { CK(L::cols(zt, N, band0, band1, tw, win, amp, 1, N, -1, -1, -1, st, duv, true, s)); });
+        timed(c, s, ST_QUAD, [&] { CK(L::quads(win, amp, 1, N, C, st, quads, qcap, -1, -1, -1, s)); });
         typename L::VisArgs a;
         a.spec = win;
+        a.amp = amp;
+        a.quads = quads;
+        a.quad_cap = qcap;
+        a.phase_tab = c.phase_tab;
         a.s_row = 1;
         a.s_col = N;
         a.nrow = N;
@@ -294,7 +352,7 @@ template <typename T> struct Pipe {
         a.partials = chi2 ? partials : nullptr;
         a.chi2_out = chi2_out;
         a.state = st;
-        if (nd > 0) CK(L::vis(a, s));
+        if (nd > 0) timed(c, s, ST_VIS, [&] { CK(L::vis(a, s)); });
     }
 };
 
@@ -349,12 +407,14 @@ template <typename T> struct Api {
         T* im_d = as<T>(c.im, (size_t)nd);
         T* w_d = as<T>(c.w, (size_t)nd);
         DevState* st = as<DevState>(c.state, 1);
-        h2d(img_d, img, sizeof(T) * (size_t)N * N, s);
-        h2d(u_d, u, sizeof(T) * (size_t)nd, s);
-        h2d(v_d, v, sizeof(T) * (size_t)nd, s);
-        h2d(re_d, re, sizeof(T) * (size_t)nd, s);
-        h2d(im_d, im, sizeof(T) * (size_t)nd, s);
-        h2d(w_d, w, sizeof(T) * (size_t)nd, s);
+        timed(c, s, ST_H2D, [&] {
+            h2d(img_d, img, sizeof(T) * (size_t)N * N, s);
+            h2d(u_d, u, sizeof(T) * (size_t)nd, s);
+            h2d(v_d, v, sizeof(T) * (size_t)nd, s);
+            h2d(re_d, re, sizeof(T) * (size_t)nd, s);
+            h2d(im_d, im, sizeof(T) * (size_t)nd, s);
+            h2d(w_d, w, sizeof(T) * (size_t)nd, s);
+        });
         CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
         Pipe<T>::enqueue(c, s, N, (double)duv, img_d, nullptr, 0, 0, 0, 0, 0, nullptr, (double)v_origin, (double)dRA,
                          (double)dDec, (double)PA, nd, u_d, v_d, re_d, im_d, w_d, nullptr, true, nullptr, st, false);
@@ -404,12 +464,14 @@ template <typename T> struct Api {
         T* im_d = as<T>(c.im, (size_t)nd);
         T* w_d = as<T>(c.w, (size_t)nd);
         DevState* st = as<DevState>(c.state, 1);
-        h2d(I_d, I, sizeof(T) * (size_t)nr, s);
-        h2d(u_d, u, sizeof(T) * (size_t)nd, s);
-        h2d(v_d, v, sizeof(T) * (size_t)nd, s);
-        h2d(re_d, re, sizeof(T) * (size_t)nd, s);
-        h2d(im_d, im, sizeof(T) * (size_t)nd, s);
-        h2d(w_d, w, sizeof(T) * (size_t)nd, s);
+        timed(c, s, ST_H2D, [&] {
+            h2d(I_d, I, sizeof(T) * (size_t)nr, s);
+            h2d(u_d, u, sizeof(T) * (size_t)nd, s);
+            h2d(v_d, v, sizeof(T) * (size_t)nd, s);
+            h2d(re_d, re, sizeof(T) * (size_t)nd, s);
+            h2d(im_d, im, sizeof(T) * (size_t)nd, s);
+            h2d(w_d, w, sizeof(T) * (size_t)nd, s);
+        });
         CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
         Pipe<T>::enqueue(c, s, N, (double)duv, nullptr, I_d, nr, Rmin, dR, dxy, inc, &pg, 1.0, dRA, dDec, PA, nd, u_d,
                          v_d, re_d, im_d, w_d, nullptr, true, nullptr, st, false);
@@ -426,7 +488,6 @@ template <typename T> struct Api {
         ProfileGeom pg = profile_geom<T>(I_host, nr, Rmin, dR, dxy, nxy);
         Ctx& c = ctx();
         std::lock_guard<std::mutex> lk(c.mu);
-        if (!s) s = c.stream;
         DevState* st = as<DevState>(c.state, 1);
         CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
         Pipe<T>::enqueue(c, s, nxy, (double)duv, nullptr, I_d, nr, Rmin, dR, dxy, inc, &pg, 1.0, dRA, dDec, PA, nd,
@@ -440,7 +501,6 @@ template <typename T> struct Api {
         check_nd(nd);
         Ctx& c = ctx();
         std::lock_guard<std::mutex> lk(c.mu);
-        if (!s) s = c.stream;
         DevState* st = as<DevState>(c.state, 1);
         CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
         Pipe<T>::enqueue(c, s, nx, (double)duv, img_d, nullptr, 0, 0, 0, 0, 0, nullptr, (double)v_origin, dRA, dDec,
@@ -513,6 +573,10 @@ template <typename T> struct Api {
         CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
         typename L::VisArgs a;
         a.spec = spec;
+        a.amp = nullptr;
+        a.quads = nullptr;
+        a.quad_cap = 0;
+        a.phase_tab = c.phase_tab;
         a.s_row = ncol;
         a.s_col = 1;
         a.nrow = nrow;
@@ -598,7 +662,7 @@ template <typename T> struct Api {
                              s));
         const CT* tw = c.twiddles<T>(N);
         CK(L::rows_image(img_d, N, tw, zt, C, st, 1.0, false, s));
-        CK(L::cols(zt, N, 0, N, tw, out, C, 1, C, 0, N, st, 1.0, false, s));
+        CK(L::cols(zt, N, 0, N, tw, out, nullptr, C, 1, C, 0, N, st, 1.0, false, s));
         d2h(data, out, sizeof(CT) * (size_t)N * C, s);
         CK(cudaStreamSynchronize(s));
     }
@@ -746,6 +810,39 @@ API int galario_cleanup(void) {
 
 GALARIO_DEFINE(double, _d)
 GALARIO_DEFINE(float, _f)
+
+API int galario_stage_timing(int enable) {
+    return guarded([&] {
+        gbg::Ctx& c = gbg::ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        c.timing = enable != 0;
+    });
+}
+API const char* galario_stage_name(int stage) {
+    return (stage >= 0 && stage < gbg::ST_COUNT) ? gbg::kStageNames[stage] : "";
+}
+API int galario_stage_times(double* ms_sum, int* count, int nstages) {
+    return guarded([&] {
+        gbg::Ctx& c = gbg::ctx();
+        std::lock_guard<std::mutex> lk(c.mu);
+        for (int i = 0; i < nstages; ++i) {
+            ms_sum[i] = 0.;
+            count[i] = 0;
+        }
+        for (auto& r : c.recs) {
+            gbg::cuda_check(cudaEventSynchronize(r.b), "cudaEventSynchronize");
+            float ms = 0.f;
+            gbg::cuda_check(cudaEventElapsedTime(&ms, r.a, r.b), "cudaEventElapsedTime");
+            if (r.stage < nstages) {
+                ms_sum[r.stage] += ms;
+                count[r.stage] += 1;
+            }
+            c.spare.push_back(r.a);
+            c.spare.push_back(r.b);
+        }
+        c.recs.clear();
+    });
+}
 
 API int galario_device_status(unsigned int* err_bits) {
     return guarded([&] {

@@ -28,8 +28,10 @@ struct DevState {
     double chi2;                  // final chi2 (written by the last reduction block)
     unsigned int err;             // error bits, see ERR_*
     unsigned int ticket;          // last-block-done counter of the chi2 reduction
-    unsigned long long err_index; // first offending visibility index (best effort)
-    double pad[4];
+    unsigned long long err_index; // first offending visibility index + 1 (best effort)
+    int win_K, win_r0, win_W;     // spectrum window, written once by the extent pass
+    unsigned int ticket_extent;   // last-block-done counter of the extent pass
+    double pad[2];
 };
 
 enum : unsigned int {
@@ -49,7 +51,7 @@ __host__ __device__ inline Window window_from_extent(double rmax2, double duv, i
     const int C = N / 2 + 1;
     Window w;
     double ext = sqrt(rmax2) / duv;
-    ext = ext * (1.0 + 1e-9) + 1e-9;           // rotation/rounding margin
+    ext = ext * (1.0 + 2e-6) + 1e-6;           // rotation/rounding margin (covers a float-precision max)
     if (!(ext < 4.0 * N)) ext = 4.0 * N;       // NaN/inf/huge: clamp (points get flagged later)
     int fu = (int)floor(ext);
     int K = fu + 2;                             // fl_u and fl_u + 1
@@ -65,6 +67,19 @@ __host__ __device__ inline Window window_from_extent(double rmax2, double duv, i
     return w;
 }
 
+// double-float value hi + lo (two floats, about 44 significant bits)
+struct DF {
+    float hi, lo;
+};
+
+// reals per cell record of the quad layout (8 for the corners, 4 moduli, 4 padding)
+constexpr int QUAD_REC = 16;
+// cells of the quad buffer (2^21: 128 MiB in FP32, 256 MiB in FP64)
+constexpr long long QUAD_CAP = 1LL << 21;
+
+// size of the table of the table-driven sin/cos of the phase shift
+constexpr int PHASE_T = 1024;
+
 inline bool is_pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
 
 // ---------------------------------------------------------------------------
@@ -73,7 +88,8 @@ inline bool is_pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
 template <typename T> struct Launch {
     using CT = C2<T>;
     // dataset extent: state->rmax2 = max(u^2 + v^2)
-    static cudaError_t extent(const T* u, const T* v, int nd, DevState* state, cudaStream_t s);
+    // ... and the window (state->win_*) derived from it for an N x N image with cell duv
+    static cudaError_t extent(const T* u, const T* v, int nd, int N, double duv, DevState* state, cudaStream_t s);
     // row pass on an image (rows [0, N)), output zt for columns [0, K) where
     // K = host_K if >= 0, else from state->rmax2 (window_from_extent).
     // row_sign: multiply row i by (-1)^i.
@@ -87,12 +103,18 @@ template <typename T> struct Launch {
     // write rows [r0, r0+W) of columns [0, K) to out[(r - r0)*s_row + k*s_col],
     // times (-1)^(r + k + N/2) if out_sign.  host_K/host_r0/host_W >= 0 override
     // the device-derived window.
-    static cudaError_t cols(const CT* zt, int N, int band0, int band1, const CT* tw, CT* out, long long s_row,
-                            long long s_col, int host_K, int host_r0, int host_W, const DevState* state, double duv,
-                            bool out_sign, cudaStream_t s);
+    // amp_out (optional, same layout as out) receives |out|, so the visibility
+    // pass gathers amplitudes instead of recomputing 4 moduli per point.
+    static cudaError_t cols(const CT* zt, int N, int band0, int band1, const CT* tw, CT* out, T* amp_out,
+                            long long s_row, long long s_col, int host_K, int host_r0, int host_W,
+                            const DevState* state, double duv, bool out_sign, cudaStream_t s);
     // fused rotation + interpolation + phase + (vis out) + (chi2 reduction)
     struct VisArgs {
         const CT* spec;      // spectrum window
+        const T* amp;        // |spec| in the same layout, or null (computed on the fly)
+        const T* quads;      // cell-major records (see Launch::quads), or null: gather from spec/amp
+        long long quad_cap;  // capacity of quads in cells; larger windows gather from spec/amp
+        const double2* phase_tab;  // exp(2 pi i (j - PHASE_T/2) / PHASE_T), j in [0, PHASE_T]; FP64 path
         long long s_row, s_col;
         int nrow, ncol;      // logical N and C of the full spectrum (flat-index semantics)
         int host_K, host_r0, host_W;  // window (>= 0) or derive from state
@@ -100,6 +122,27 @@ template <typename T> struct Launch {
         bool rotate;         // PA != 0
         double dra, ddec;    // rotated offsets (radians, not yet times 2 pi)
         bool phase;          // dra != 0 || ddec != 0
+        // derived on the host by finalize(): no per-thread FP64 set-up in the kernels
+        double inv_duv, half_nrow;
+        float half_nrow_f, v_origin_f;
+        DF inv_duv_df, cpa, spa, dra_df, ddec_df;  // double-float copies for the FP32 path
+        void finalize() {
+            auto split = [](double x) {
+                DF r;
+                r.hi = (float)x;
+                r.lo = (float)(x - (double)r.hi);
+                return r;
+            };
+            inv_duv = 1.0 / duv;
+            half_nrow = (double)(nrow / 2);
+            half_nrow_f = (float)(nrow / 2);
+            v_origin_f = (float)v_origin;
+            inv_duv_df = split(inv_duv);
+            cpa = split(cos_pa);
+            spa = split(sin_pa);
+            dra_df = split(dra);
+            ddec_df = split(ddec);
+        }
         const T *u, *v, *re, *im, *w;
         int nd;
         CT* vis_out;         // may be null
@@ -108,6 +151,18 @@ template <typename T> struct Launch {
         DevState* state;
     };
     static cudaError_t vis(const VisArgs& a, cudaStream_t s);
+    // Cell-major copy of the window for the visibility gather: one record of
+    // QUAD_REC reals per cell (k, r), k in [0, K), r in [r0, r0 + W), at
+    // quads + (k * W + (r - r0)) * QUAD_REC, holding the cell's 4 bilinear
+    // corners y0 = S[r][k], y1 = S[r+1][k], y2 = S[r+1][k+1], y3 = S[r][k+1]
+    // (complex, re/im) then their 4 moduli.  At k = C-1 the corners k+1 are
+    // taken from column 0 of the next rows, as the reference's flat indexing
+    // does.  Cells whose corners fall outside the window are left unwritten
+    // and never read.
+    // A window of more than `cap` cells is not converted (the gather then falls back to spec/amp).
+    static cudaError_t quads(const CT* spec, const T* amp, long long s_row, long long s_col, int C,
+                             const DevState* state, T* quads, long long cap, int host_K, int host_r0, int host_W,
+                             cudaStream_t s);
     static int vis_grid(int nd);
     // expert-stage kernels
     static cudaError_t fftshift_real(T* padded, int N, cudaStream_t s);

@@ -101,7 +101,7 @@ int galario_chi2_profile_f(int nr, const float *intensity, float Rmin, float dR,
  * All *_dev pointers are device pointers; intensity_host is the same profile
  * in host memory (the central pixel is integrated on the host, as in the
  * reference :1136-1153).  The call only enqueues work on `stream` (a
- * cudaStream_t, or NULL for the library's stream) and writes chi2 as a double
+ * cudaStream_t; NULL is CUDA's default stream) and writes chi2 as a double
  * to chi2_dev; galario_device_status() synchronises and reports device-side
  * errors.  Calls on one device share a workspace: issue them on one stream. */
 int galario_chi2_profile_device_d(int nr, const double *intensity_host, const double *intensity_dev, double Rmin,
@@ -122,6 +122,17 @@ int galario_chi2_image_device_f(int nx, int ny, const float *image_dev, float v_
                                 void *stream);
 /* Synchronise the device and return the error bits of the last device-resident call. */
 int galario_device_status(unsigned int *err_bits);
+
+/* ---- stage timing (no reference counterpart; the reference's compile-time
+ * GALARIO_TIMING prints, src/galario.cpp:64-87,275-315, become queryable
+ * CUDA-event times).  With timing enabled every pipeline stage of the calls
+ * on this device is bracketed by CUDA events on its stream; stage ids:
+ * 0 h2d, 1 extent, 2 rows, 3 cols, 4 vis, 5 d2h, 6 quad. ---- */
+int galario_stage_timing(int enable);
+const char *galario_stage_name(int stage);
+/* Synchronise, then return per stage the summed milliseconds and the number of
+ * timed launches since the previous query (arrays of nstages entries). */
+int galario_stage_times(double *ms_sum, int *count, int nstages);
 
 /* ---- expert stages (reference src/galario_py.h:36-46, python/libcommon.pyx:800-1082) ---- */
 
