@@ -177,6 +177,19 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+def profiled_traffic(stage: str, precision: str):
+    """DRAM bytes per launch of a kernel from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) == 3 and not line.startswith("#") and parts[0] == stage and parts[1] == precision:
+                return float(parts[2])
+    return None
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -388,7 +401,8 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h_bytes, "api": "galario_gb300.double.chi2Profile, pinned numpy inputs"},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                         "traffic": None, "algorithmic_bytes": alg[dom],
+                         "traffic": profiled_traffic(dom, "f64"), "algorithmic_bytes": alg[dom],
+                         "traffic_source": "profiles/dram_traffic.txt (ncu dram__bytes_read+write of one launch)",
                          "note": "FP64 arithmetic on GB300 runs at ~1.2 TFLOP/s; the FP64 kernels are "
                                  "FP64-issue-bound, not HBM-bound"},
             "stages_ms": {k: round(v, 4) for k, v in stages64.items()},
