@@ -698,6 +698,11 @@ template <typename T> struct Api {
 }  // namespace
 }  // namespace gbg
 
+namespace gbg {
+// message for galario_last_error() from entry points defined in other translation units
+void set_error_message(const std::string& msg) { g_msg = msg; }
+}  // namespace gbg
+
 using gbg::Api;
 using gbg::guarded;
 

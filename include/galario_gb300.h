@@ -123,6 +123,24 @@ int galario_chi2_image_device_f(int nx, int ny, const float *image_dev, float v_
 /* Synchronise the device and return the error bits of the last device-resident call. */
 int galario_device_status(unsigned int *err_bits);
 
+/* ---- allocation-free chi2 reduction (no counterpart in the reference) ----
+ * For callers that cannot let this library allocate GPU memory: device memory
+ * owned by another allocator (PyTorch's caching allocator, a pool sized at
+ * start-up) or loops that cannot afford the device-wide synchronisation of
+ * cudaFree.  Computes chi2 = sum_k w_k |vis_k - (re_k + i im_k)|^2 (double,
+ * accumulated in double) of caller-owned DEVICE arrays and writes it to
+ * chi2_dev (device memory); only enqueues work on `stream` (NULL: CUDA's
+ * default stream).  It calls no cudaMalloc/cudaFree: its scratch is a fixed
+ * 32 KiB array inside the library's device image, held by every GPU that
+ * loads the library until exit.
+ *  - nd <= 16,777,216, otherwise GALARIO_EINVAL;
+ *  - the first call on a device (with it current) looks up the scratch
+ *    address once; make that first call before any stream capture;
+ *  - all calls share the scratch: calls whose kernels overlap on the GPU
+ *    race; order them on one stream. */
+int galario_reduce_chi2_noalloc_d(int nd, const double *re_dev, const double *im_dev, const double *vis_dev,
+                                  const double *w_dev, double *chi2_dev, void *stream);
+
 /* ---- stage timing (no reference counterpart; the reference's compile-time
  * GALARIO_TIMING prints, src/galario.cpp:64-87,275-315, become queryable
  * CUDA-event times).  With timing enabled every pipeline stage of the calls
