@@ -1,0 +1,969 @@
+// Batched FP32 chi2 of B radial-profile models against one device-resident
+// dataset, with the gradient of every chi2 with respect to the profile
+// samples, the inclination, the position angle and the offsets.
+//
+// Forward (per model b, all models in the same launches):
+//   model_setup   per-model constants (rotation, offsets, 1/cos inc, central pixel)
+//   rows          sweep fused into the shared-memory real FFT of each non-zero image row
+//   cols          column FFT of the K needed columns -> window rows, moduli
+//   quads         cell-major corner records of the window
+//   vis           for every visibility, all B models: double-float index and
+//                 phase, bilinear amp/phase interpolation, residual, chi2
+// Adjoint (reverse mode; the spectrum is recomputed by the forward launches
+// of the same call, not stored between calls):
+//   vis           dchi2/dV = 2 w (V - obs) -> through the phase shift (dRA,
+//                 dDec), the modulus/argument interpolation (cell-corner
+//                 gradients, scattered with float4 atomics into per-cell
+//                 records) and the interpolation position (PA)
+//   quadT         per-cell records -> gradient of every window element,
+//                 plus the modulus part times S/|S|, times the output sign
+//   colsT         inverse column FFT (the adjoint of the forward column FFT)
+//   rowsT         inverse real FFT of each image row with Hermitian weights
+//                 (the adjoint of the R2C row transform), times the row sign,
+//                 fused with the adjoint of the sweep (profile samples, inc)
+//   central       adjoint of the central-pixel average
+// Reference semantics followed: sweep_core src/galario.cpp:1048-1071, central
+// pixel :1136-1153, interpolate_core :749-815, apply_phase_sampled_core
+// :877-884, uv_rotate_core :955-960, reduce_chi2 :1504-1538.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/galario_gb300.h"
+#include "gb_device.cuh"
+#include "gb_internal.cuh"
+
+namespace gbg {
+void set_error_message(const std::string& msg);  // gb_api.cu
+
+namespace {
+
+constexpr int kPts = 4;        // visibilities per thread in the vis pass
+constexpr int kVisThreads = 256;
+constexpr int kRowsPerCta = 4;  // image rows per CTA in the row adjoint
+constexpr int kRec = 16;        // floats per forward cell record (QUAD_REC)
+constexpr int kGRec = 12;       // floats per gradient cell record
+
+struct ModelConst {
+    DF cpa, spa;          // cos / sin PA
+    DF dra, ddec;         // rotated offsets (radians)
+    float inv_cos_inc;    // 1 / cos(inc)
+    float tan_inc;        // tan(inc)
+    float central;        // central pixel value (Jy/pixel)
+    int rotate, phase;
+    float pad[3];
+};
+
+struct Geo {  // geometry shared by all models of a batch
+    int N, M, C, K, r0, W, rmax, band0, R, nr, iIN;
+    float Rmin, dR, inv_dR, dxy, sr_to_px;
+    float inv_duv_hi, inv_duv_lo, half_nrow;
+    float vo;  // v_origin: profiles use origin 'upper' (+1)
+};
+
+// ---------------------------------------------------------------------------
+// forward kernels
+// ---------------------------------------------------------------------------
+__global__ void model_setup_kernel(int B, const float* __restrict__ params, const float* __restrict__ intensity,
+                                   int nr, const double* __restrict__ central_coef, int ncoef, ModelConst* mc) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const double inc = params[4 * b + 0], PA = params[4 * b + 1];
+    const double dRA = params[4 * b + 2], dDec = params[4 * b + 3];
+    ModelConst m;
+    auto split = [](double x) {
+        DF r;
+        r.hi = (float)x;
+        r.lo = (float)(x - (double)r.hi);
+        return r;
+    };
+    const double c = cos(PA), s = sin(PA);
+    m.rotate = (PA != 0.0);
+    m.cpa = split(m.rotate ? c : 1.0);
+    m.spa = split(m.rotate ? s : 0.0);
+    const double dra = m.rotate ? dRA * c - dDec * s : dRA;
+    const double ddec = m.rotate ? dRA * s + dDec * c : dDec;
+    m.dra = split(dra);
+    m.ddec = split(ddec);
+    m.phase = !(dra == 0.0 && ddec == 0.0);
+    const double ci = cos(inc);
+    m.inv_cos_inc = (float)(1.0 / ci);
+    m.tan_inc = (float)tan(inc);
+    double cen = 0.0;
+    const float* I = intensity + (size_t)b * nr;
+    for (int i = 0; i < ncoef; ++i) cen += central_coef[i] * (double)I[i];
+    m.central = (float)cen;
+    m.pad[0] = m.pad[1] = m.pad[2] = 0.f;
+    mc[b] = m;
+}
+
+template <int E>
+__global__ void __launch_bounds__(1024) rows_batch_kernel(Geo g, const float* __restrict__ intensity,
+                                                          const ModelConst* __restrict__ mc,
+                                                          const float2* __restrict__ tw, float2* __restrict__ zt) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* buf = reinterpret_cast<float2*>(smem_raw);
+    const int b = blockIdx.y;
+    const int irow = blockIdx.x;
+    const int I = g.band0 + irow;
+    const int off = g.N / 2 - g.rmax;
+    const float* Ib = intensity + (size_t)b * g.nr;
+    const ModelConst m = mc[b];
+    for (int mm = threadIdx.x; mm < g.M; mm += blockDim.x) {
+        const int J0 = 2 * mm, J1 = 2 * mm + 1;
+        float a = sweep_pixel<float>(I, J0, Ib, g.nr, g.Rmin, g.dR, g.inv_dR, g.dxy, m.inv_cos_inc, g.rmax, off,
+                                     g.sr_to_px);
+        float c = sweep_pixel<float>(I, J1, Ib, g.nr, g.Rmin, g.dR, g.inv_dR, g.dxy, m.inv_cos_inc, g.rmax, off,
+                                     g.sr_to_px);
+        if (I == g.N / 2) {
+            if (J0 == g.N / 2) a = m.central;
+            if (J1 == g.N / 2) c = m.central;
+        }
+        buf[mm] = make_float2(a, c);
+    }
+    __syncthreads();
+    block_fft<float, E>(buf, g.M, ilog2(g.M), tw, 2);
+    const float sgn = (I & 1) ? -1.f : 1.f;
+    float2* out = zt + (size_t)b * g.K * g.R;
+    for (int k = threadIdx.x; k < g.K; k += blockDim.x) {
+        const float2 x = real_split<float>(buf, g.M, k, tw);
+        out[(size_t)k * g.R + irow] = make_float2(sgn * x.x, sgn * x.y);
+    }
+}
+
+template <int E>
+__global__ void __launch_bounds__(1024) cols_batch_kernel(Geo g, const float2* __restrict__ zt,
+                                                          const float2* __restrict__ tw, float2* __restrict__ win,
+                                                          float* __restrict__ amp) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* buf = reinterpret_cast<float2*>(smem_raw);
+    const int b = blockIdx.y, k = blockIdx.x;
+    const float2* col = zt + ((size_t)b * g.K + k) * g.R;
+    for (int i = threadIdx.x; i < g.N; i += blockDim.x) {
+        const int q = i - g.band0;
+        buf[i] = (q >= 0 && q < g.R) ? __ldg(&col[q]) : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    block_fft<float, E>(buf, g.N, ilog2(g.N), tw, 1);
+    const int par = (k + g.N / 2) & 1;
+    float2* wcol = win + ((size_t)b * g.K + k) * g.W;
+    float* acol = amp + ((size_t)b * g.K + k) * g.W;
+    for (int q = threadIdx.x; q < g.W; q += blockDim.x) {
+        const int r = g.r0 + q;
+        float2 x = buf[r];
+        if ((r & 1) ^ par) x = make_float2(-x.x, -x.y);
+        wcol[q] = x;
+        acol[q] = sqrtf(fmaf(x.x, x.x, x.y * x.y));
+    }
+}
+
+// cell (k, q) corners in the window (see Launch::quads): returns false when a
+// corner falls outside the window
+__device__ __forceinline__ bool cell_corners(const Geo& g, int k, int q, int* rr, int* cc) {
+    const bool wrap = (k + 1 == g.C);
+    rr[0] = q;
+    rr[1] = q + 1;
+    rr[2] = wrap ? q + 2 : q + 1;
+    rr[3] = wrap ? q + 1 : q;
+    cc[0] = k;
+    cc[1] = k;
+    cc[2] = wrap ? 0 : k + 1;
+    cc[3] = wrap ? 0 : k + 1;
+    bool ok = true;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) ok = ok && rr[c] < g.W && cc[c] < g.K;
+    return ok;
+}
+
+__global__ void quad_batch_kernel(Geo g, int B, const float2* __restrict__ win, const float* __restrict__ amp,
+                                  float* __restrict__ quads) {
+    const long long ncell = (long long)g.K * g.W;
+    const long long total = ncell * B;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(e / ncell);
+        const long long cell = e - (long long)b * ncell;
+        const int k = (int)(cell / g.W), q = (int)(cell - (long long)k * g.W);
+        int rr[4], cc[4];
+        if (!cell_corners(g, k, q, rr, cc)) continue;
+        const float2* wb = win + (size_t)b * ncell;
+        const float* ab = amp + (size_t)b * ncell;
+        float rec[12];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const long long o = (long long)cc[c] * g.W + rr[c];
+            const float2 y = wb[o];
+            rec[2 * c] = y.x;
+            rec[2 * c + 1] = y.y;
+            rec[8 + c] = ab[o];
+        }
+        float4* dst = reinterpret_cast<float4*>(quads + e * kRec);
+        dst[0] = make_float4(rec[0], rec[1], rec[2], rec[3]);
+        dst[1] = make_float4(rec[4], rec[5], rec[6], rec[7]);
+        dst[2] = make_float4(rec[8], rec[9], rec[10], rec[11]);
+    }
+}
+
+// One (visibility, model) evaluation with the intermediates the adjoint needs.
+struct PointEval {
+    float2 V;              // model visibility
+    float2 y[4];           // cell corners
+    float am[4];           // corner moduli
+    float t, q, su;        // fractions along v and u, sign of u'
+    float A, zr, zi, rn;   // interpolated modulus, complex bilinear, 1/|z|
+    float pc, ps;          // phase factor
+    float ur, vr;          // rotated u, v (float)
+    long long cell;        // cell index in the model's window, -1 if none
+    unsigned err;
+};
+
+__device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, const float* __restrict__ quads_b,
+                                           float u, float v, PointEval& p) {
+    p.V = make_float2(0.f, 0.f);
+    p.cell = -1;
+    p.err = 0u;
+    if (!(isfinite(u) && isfinite(v))) {
+        p.err = ERR_UV_NONFINITE;
+        return;
+    }
+    DF ur = DF{u, 0.f}, vr = DF{v, 0.f};
+    if (m.rotate) {
+        ur = df_add(df_mul_f(u, m.cpa), df_neg(df_mul_f(v, m.spa)));
+        vr = df_add(df_mul_f(u, m.spa), df_mul_f(v, m.cpa));
+    }
+    p.ur = ur.hi;
+    p.vr = vr.hi;
+    const float su = copysignf(1.f, ur.hi);
+    p.su = su;
+    const DF inv_duv = DF{g.inv_duv_hi, g.inv_duv_lo};
+    const DF au = ur.hi < 0.f ? df_neg(ur) : ur;
+    const DF indu = df_mul(au, inv_duv);
+    const DF sv = (g.vo * su < 0.f) ? df_neg(vr) : vr;
+    const DF indv = df_add(DF{g.half_nrow, 0.f}, df_mul(sv, inv_duv));
+    const float lim = 8.f * g.half_nrow;
+    if (!(indu.hi < lim && indv.hi > -lim && indv.hi < lim)) {
+        p.err = ERR_UV_OUTSIDE;
+        return;
+    }
+    int fu, fv;
+    df_floor(indu, &fu, &p.q);
+    df_floor(indv, &fv, &p.t);
+    int r0 = fv, c0 = fu;
+    while (c0 >= g.C) {
+        c0 -= g.C;
+        r0 += 1;
+    }
+    const bool wrap = (c0 + 1 == g.C);
+    if (r0 < 0 || (wrap ? r0 + 2 : r0 + 1) >= g.N) {
+        p.err = ERR_UV_OUTSIDE;
+        return;
+    }
+    const int qq = r0 - g.r0;
+    const bool inside = wrap ? (g.K == g.C && qq >= 0 && qq < g.W - 2) : (c0 < g.K - 1 && qq >= 0 && qq < g.W - 1);
+    if (!inside) {
+        p.err = ERR_WINDOW;
+        return;
+    }
+    p.cell = (long long)c0 * g.W + qq;
+    const float4* rec = reinterpret_cast<const float4*>(quads_b + p.cell * kRec);
+    const float4 p0 = __ldg(rec), p1 = __ldg(rec + 1), p2 = __ldg(rec + 2);
+    p.y[0] = make_float2(p0.x, p0.y);
+    p.y[1] = make_float2(p0.z, p0.w);
+    p.y[2] = make_float2(p1.x, p1.y);
+    p.y[3] = make_float2(p1.z, p1.w);
+    p.am[0] = p2.x;
+    p.am[1] = p2.y;
+    p.am[2] = p2.z;
+    p.am[3] = p2.w;
+    const float t = p.t, q = p.q;
+    const float d1r = (p.y[0].x + p.y[2].x) - (p.y[1].x + p.y[3].x);
+    const float d1i = (p.y[0].y + p.y[2].y) - (p.y[1].y + p.y[3].y);
+    p.zr = t * (q * d1r) + (t * (p.y[1].x - p.y[0].x) + q * (p.y[3].x - p.y[0].x)) + p.y[0].x;
+    p.zi = t * (q * d1i) + (t * (p.y[1].y - p.y[0].y) + q * (p.y[3].y - p.y[0].y)) + p.y[0].y;
+    float A = p.am[0];
+    A += (p.am[3] - p.am[0]) * q;
+    A += (p.am[1] - p.am[0]) * t;
+    A += (p.am[0] - p.am[1] + p.am[2] - p.am[3]) * t * q;
+    p.A = A;
+    float cph = 1.f, sph = 0.f;
+    p.rn = 0.f;
+    if (p.zr != 0.f || p.zi != 0.f) {
+        p.rn = rsqrtf(fmaf(p.zr, p.zr, p.zi * p.zi));
+        cph = p.zr * p.rn;
+        sph = su * p.zi * p.rn;
+    }
+    float2 U = make_float2(A * cph, A * sph);
+    p.pc = 1.f;
+    p.ps = 0.f;
+    if (m.phase) {
+        const DF ph = df_add(df_mul(ur, m.dra), df_mul(vr, m.ddec));
+        float n;
+        if (fabsf(ph.hi) < 4194304.f) rint_i(ph.hi, &n);
+        else n = rintf(ph.hi);
+        const float f = __fadd_rn(__fsub_rn(ph.hi, n), ph.lo);
+        sincos2pi_f32(f, &p.ps, &p.pc);
+        U = make_float2(U.x * p.pc - U.y * p.ps, U.x * p.ps + U.y * p.pc);
+    }
+    p.V = U;
+}
+
+// Accumulators per model and block: chi2, dPA, dRA, dDec
+constexpr int kAcc = 4;
+
+template <bool GRAD>
+__global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, int nd, const float* __restrict__ u,
+                                                                const float* __restrict__ v,
+                                                                const float* __restrict__ re,
+                                                                const float* __restrict__ im,
+                                                                const float* __restrict__ w,
+                                                                const ModelConst* __restrict__ mc,
+                                                                const float* __restrict__ quads,
+                                                                float* __restrict__ cgrad, double* __restrict__ partials,
+                                                                DevState* st) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ModelConst* smc = reinterpret_cast<ModelConst*>(smem_raw);
+    double* sacc = reinterpret_cast<double*>(smc + B);  // [B][kAcc]
+    __shared__ float red[kAcc][kVisThreads / 32];
+    for (int i = threadIdx.x; i < B; i += blockDim.x) smc[i] = mc[i];
+    for (int i = threadIdx.x; i < B * kAcc; i += blockDim.x) sacc[i] = 0.0;
+    // this thread's points
+    float pu[kPts], pv[kPts], pre[kPts], pim[kPts], pw[kPts];
+    const long long base = (long long)blockIdx.x * kVisThreads * kPts + threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < kPts; ++j) {
+        const long long i = base + (long long)j * kVisThreads;
+        const bool in = i < nd;
+        pu[j] = in ? __ldg(&u[i]) : 0.f;
+        pv[j] = in ? __ldg(&v[i]) : 0.f;
+        pre[j] = in ? __ldg(&re[i]) : 0.f;
+        pim[j] = in ? __ldg(&im[i]) : 0.f;
+        pw[j] = in ? __ldg(&w[i]) : 0.f;  // w = 0 marks the padding points
+    }
+    __syncthreads();
+    const long long ncell = (long long)g.K * g.W;
+    unsigned err = 0u;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int b = 0; b < B; ++b) {
+        const ModelConst m = smc[b];
+        const float* qb = quads + (size_t)b * ncell * kRec;
+        float acc[kAcc] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int j = 0; j < kPts; ++j) {
+            if (pw[j] == 0.f) continue;
+            PointEval p;
+            eval_point(g, m, qb, pu[j], pv[j], p);
+            err |= p.err;
+            const float dr = p.V.x - pre[j], di = p.V.y - pim[j];
+            acc[0] += pw[j] * (dr * dr + di * di);
+            if (GRAD && p.cell >= 0) {
+                // dchi2/dV
+                const float gx = 2.f * pw[j] * dr, gy = 2.f * pw[j] * di;
+                // phase shift V = U P: dchi2/dphi = -Im(conj(G) V); phi = 2 pi (u dRA + v dDec)
+                const float dphi = -(gx * p.V.y - gy * p.V.x);
+                acc[2] += dphi * 6.28318530717958647692f * pu[j];
+                acc[3] += dphi * 6.28318530717958647692f * pv[j];
+                // G_U = G conj(P)
+                const float gux = gx * p.pc + gy * p.ps, guy = -gx * p.ps + gy * p.pc;
+                // U = A * (zr, su zi) / |z|
+                const float ex = p.zr * p.rn, ey = p.zi * p.rn;  // e = z/|z|
+                const float gA = gux * ex + guy * (p.su * ey);
+                // gradient w.r.t. e (undo the conjugation for u < 0)
+                const float gex = p.A * gux, gey = p.su * p.A * guy;
+                const float dot = ex * gex + ey * gey;
+                const float gzx = (gex - ex * dot) * p.rn, gzy = (gey - ey * dot) * p.rn;
+                const float t = p.t, q = p.q;
+                const float wgt[4] = {(1.f - t) * (1.f - q), t * (1.f - q), t * q, (1.f - t) * q};
+                float4* dst = reinterpret_cast<float4*>(cgrad + ((size_t)b * ncell + p.cell) * kGRec);
+                atomicAdd(dst, make_float4(wgt[0] * gzx, wgt[0] * gzy, wgt[1] * gzx, wgt[1] * gzy));
+                atomicAdd(dst + 1, make_float4(wgt[2] * gzx, wgt[2] * gzy, wgt[3] * gzx, wgt[3] * gzy));
+                atomicAdd(dst + 2, make_float4(wgt[0] * gA, wgt[1] * gA, wgt[2] * gA, wgt[3] * gA));
+                // position: q = |u'|/duv, t = N/2 + vo su v'/duv; du'/dPA = -v', dv'/dPA = u'
+                const float dzqx = (p.y[3].x - p.y[0].x) + t * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
+                const float dzqy = (p.y[3].y - p.y[0].y) + t * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
+                const float dztx = (p.y[1].x - p.y[0].x) + q * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
+                const float dzty = (p.y[1].y - p.y[0].y) + q * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
+                const float dAq = (p.am[3] - p.am[0]) + t * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
+                const float dAt = (p.am[1] - p.am[0]) + q * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
+                const float gq = gzx * dzqx + gzy * dzqy + gA * dAq;
+                const float gt = gzx * dztx + gzy * dzty + gA * dAt;
+                const float inv_duv = g.inv_duv_hi;
+                acc[1] += gq * (p.su * (-p.vr) * inv_duv) + gt * (g.vo * p.su * p.ur * inv_duv);
+            }
+        }
+        // block reduction of this model's accumulators
+#pragma unroll
+        for (int a = 0; a < (GRAD ? kAcc : 1); ++a) {
+            float x = acc[a];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) red[a][wid] = x;
+        }
+        __syncthreads();
+        if (threadIdx.x < (GRAD ? kAcc : 1)) {
+            double s = 0.0;
+            for (int q = 0; q < kVisThreads / 32; ++q) s += (double)red[threadIdx.x][q];
+            sacc[b * kAcc + threadIdx.x] = s;
+        }
+        __syncthreads();
+    }
+    if (err) atomicOr(&st->err, err);
+    double* dst = partials + (size_t)blockIdx.x * B * kAcc;
+    for (int i = threadIdx.x; i < B * kAcc; i += blockDim.x) dst[i] = sacc[i];
+}
+
+// partials [blocks][B][kAcc] -> out[b][a] (fixed summation order)
+__global__ void batch_finalize_kernel(int B, int nblocks, const double* __restrict__ partials,
+                                      double* __restrict__ chi2, double* __restrict__ gsum) {
+    __shared__ double sh[32];
+    const int b = blockIdx.x, a = blockIdx.y;
+    double s = 0.0;
+    for (int q = threadIdx.x; q < nblocks; q += blockDim.x) s += partials[((size_t)q * B + b) * kAcc + a];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) {
+        if (a == 0) chi2[b] = s;
+        else gsum[b * kAcc + a] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// adjoint kernels
+// ---------------------------------------------------------------------------
+// gradient of every window element from the cell records; S/|S| for the
+// modulus part; times the forward output sign
+__global__ void quadT_batch_kernel(Geo g, int B, const float* __restrict__ cgrad, const float2* __restrict__ win,
+                                   const float* __restrict__ amp, float2* __restrict__ gwin) {
+    const long long ncell = (long long)g.K * g.W;
+    const long long total = ncell * B;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(e / ncell);
+        const long long el = e - (long long)b * ncell;
+        const int k = (int)(el / g.W), q = (int)(el - (long long)k * g.W);
+        const float* cg = cgrad + (size_t)b * ncell * kGRec;
+        float gx = 0.f, gy = 0.f, ga = 0.f;
+        // the element (k, q) is corner c of cell (kc, qc)
+        auto take = [&](int kc, int qc, int c) {
+            if (kc < 0 || qc < 0 || kc >= g.K || qc >= g.W) return;
+            const float* rec = cg + ((long long)kc * g.W + qc) * kGRec;
+            gx += rec[2 * c];
+            gy += rec[2 * c + 1];
+            ga += rec[8 + c];
+        };
+        take(k, q, 0);
+        take(k, q - 1, 1);
+        if (k >= 1) {
+            take(k - 1, q - 1, 2);
+            take(k - 1, q, 3);
+        } else if (g.K == g.C) {  // column 0 also serves the wrap cells of column C-1
+            take(g.C - 1, q - 2, 2);
+            take(g.C - 1, q - 1, 3);
+        }
+        const float2 s = win[(size_t)b * ncell + el];
+        const float a = amp[(size_t)b * ncell + el];
+        if (a > 0.f) {
+            gx += ga * s.x / a;
+            gy += ga * s.y / a;
+        }
+        const int r = g.r0 + q;
+        if (((r + k + g.N / 2) & 1)) {
+            gx = -gx;
+            gy = -gy;
+        }
+        gwin[(size_t)b * ncell + el] = make_float2(gx, gy);
+    }
+}
+
+// adjoint of the column pass: inverse column FFT of the window gradient, kept
+// on the band rows.  IFFT(x) = conj(FFT(conj(x))): the forward transform runs
+// on the conjugated column.
+template <int E>
+__global__ void __launch_bounds__(1024) colsT_batch_kernel(Geo g, const float2* __restrict__ gwin,
+                                                           const float2* __restrict__ tw,
+                                                           float2* __restrict__ zbar) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* buf = reinterpret_cast<float2*>(smem_raw);
+    const int b = blockIdx.y, k = blockIdx.x;
+    const float2* col = gwin + ((size_t)b * g.K + k) * g.W;
+    for (int i = threadIdx.x; i < g.N; i += blockDim.x) {
+        const int q = i - g.r0;
+        const float2 x = (q >= 0 && q < g.W) ? col[q] : make_float2(0.f, 0.f);
+        buf[i] = make_float2(x.x, -x.y);
+    }
+    __syncthreads();
+    block_fft<float, E>(buf, g.N, ilog2(g.N), tw, 1);
+    float2* out = zbar + ((size_t)b * g.K + k) * g.R;
+    for (int q = threadIdx.x; q < g.R; q += blockDim.x) {
+        const float2 x = buf[g.band0 + q];
+        out[q] = make_float2(x.x, -x.y);
+    }
+}
+
+// adjoint of the row pass + sweep: for each image row, x_bar[j] =
+// (-1)^I Re(sum_{k<K} zbar[k] e^{+2 pi i j k/N}) via the half-length inverse
+// complex FFT (Hermitian weights), then the sweep adjoint into the profile
+// and the inclination.
+template <int E>
+__global__ void __launch_bounds__(1024) rowsT_batch_kernel(Geo g, const float* __restrict__ intensity,
+                                                           const ModelConst* __restrict__ mc,
+                                                           const float2* __restrict__ tw,
+                                                           const float2* __restrict__ twc,
+                                                           const float2* __restrict__ zbar,
+                                                           float* __restrict__ gI, double* __restrict__ ginc,
+                                                           float* __restrict__ gcentral) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* buf = reinterpret_cast<float2*>(smem_raw);           // M complex
+    float* gIs = reinterpret_cast<float*>(buf + g.M);            // nr floats
+    __shared__ double shd[32];
+    __shared__ int lo_bin, hi_bin;
+    const int b = blockIdx.y;
+    const ModelConst m = mc[b];
+    const float* Ib = intensity + (size_t)b * g.nr;
+    const float2* zb = zbar + (size_t)b * g.K * g.R;
+    for (int i = threadIdx.x; i < g.nr; i += blockDim.x) gIs[i] = 0.f;
+    if (threadIdx.x == 0) {
+        lo_bin = g.nr;
+        hi_bin = -1;
+    }
+    float ginc_acc = 0.f;
+    const int off = g.N / 2 - g.rmax;
+    const int M = g.M;
+    for (int rr = 0; rr < kRowsPerCta; ++rr) {
+        const int irow = blockIdx.x * kRowsPerCta + rr;
+        if (irow >= g.R) break;  // uniform
+        const int I = g.band0 + irow;
+        __syncthreads();
+        // Hermitian weights: Y~0 = Re Y0, Y~k = Yk/2 (0<k<M), Y~M = Re YM; zero for k >= K
+        for (int k = threadIdx.x; k < M; k += blockDim.x) {
+            auto yk = [&](int kk) -> float2 {
+                if (kk >= g.K) return make_float2(0.f, 0.f);
+                const float2 y = zb[(size_t)kk * g.R + irow];
+                if (kk == 0 || kk == M) return make_float2(y.x, 0.f);
+                return make_float2(0.5f * y.x, 0.5f * y.y);
+            };
+            const float2 a = yk(k), c = yk(M - k);
+            // E' = a + conj(c), O' = (a - conj(c)) e^{+2 pi i k/N}, Z = E' + i O'
+            const float2 Ep = make_float2(a.x + c.x, a.y - c.y);
+            const float2 d = make_float2(a.x - c.x, a.y + c.y);
+            const float2 w = twc[k];  // e^{+2 pi i k / N}
+            const float2 Op = make_float2(d.x * w.x - d.y * w.y, d.x * w.y + d.y * w.x);
+            // Z = E' + i O', stored conjugated: the inverse FFT is conj(FFT(conj(Z)))
+            buf[k] = make_float2(Ep.x - Op.y, -(Ep.y + Op.x));
+        }
+        __syncthreads();
+        block_fft<float, E>(buf, M, ilog2(M), tw, 2);
+        const float sgn = (I & 1) ? -1.f : 1.f;
+        // sweep adjoint over the box pixels of this row
+        const int i_box = I - off;
+        const float y = i2f_small(g.rmax - i_box) * g.dxy;
+        for (int j = threadIdx.x; j < 2 * g.rmax; j += blockDim.x) {
+            const int J = j + off;
+            const float2 zz = buf[J >> 1];  // conj(z): x[2m] = Re z, x[2m+1] = Im z = -zz.y
+            const float xb = sgn * ((J & 1) ? -zz.y : zz.x);
+            if (I == g.N / 2 && J == g.N / 2) {  // central pixel: its own adjoint
+                gcentral[b] = xb;
+                continue;
+            }
+            const float x = i2f_small(g.rmax - j) * g.dxy;
+            const float xs = x * m.inv_cos_inc;
+            const float r = sqrtf(xs * xs + y * y);
+            const float tR = (r - g.Rmin) * g.inv_dR;
+            if (!(tR < (float)(g.nr - 1))) continue;
+            int iR = 0;
+            if (tR > 0.f) {
+                float fl;
+                iR = floor_i(tR, &fl);
+            }
+            const float frac = (r - i2f_small(iR) * g.dR - g.Rmin) * g.inv_dR;
+            const float gxs = xb * g.sr_to_px;
+            atomicAdd(&gIs[iR], gxs * (1.f - frac));
+            atomicAdd(&gIs[iR + 1], gxs * frac);
+            atomicMin(&lo_bin, iR);
+            atomicMax(&hi_bin, iR + 1);
+            if (r > 0.f) {
+                const float slope = (__ldg(&Ib[iR + 1]) - __ldg(&Ib[iR])) * g.inv_dR;
+                ginc_acc += gxs * slope * (xs * xs * m.tan_inc) / r;  // dr/dinc = xs^2 tan(inc) / r
+            }
+        }
+    }
+    __syncthreads();
+    float* gIb = gI + (size_t)b * g.nr;
+    for (int i = lo_bin + threadIdx.x; i <= hi_bin; i += blockDim.x)
+        if (gIs[i] != 0.f) atomicAdd(&gIb[i], gIs[i]);
+    const double tot = block_sum((double)ginc_acc, shd);
+    if (threadIdx.x == 0) atomicAdd(&ginc[b], tot);
+}
+
+// adjoint of the central pixel: I_bar += coef * x_bar(center)
+__global__ void central_adjoint_kernel(int B, int nr, const double* __restrict__ coef, int ncoef,
+                                       const float* __restrict__ gcentral, float* __restrict__ gI) {
+    const int b = blockIdx.x;
+    for (int i = threadIdx.x; i < ncoef; i += blockDim.x) gI[(size_t)b * nr + i] += (float)(coef[i] * gcentral[b]);
+}
+
+__global__ void write_grad_params_kernel(int B, const double* __restrict__ gsum, const double* __restrict__ ginc,
+                                         float* __restrict__ gp) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    gp[4 * b + 0] = (float)ginc[b];
+    gp[4 * b + 1] = (float)gsum[b * kAcc + 1];
+    gp[4 * b + 2] = (float)gsum[b * kAcc + 2];
+    gp[4 * b + 3] = (float)gsum[b * kAcc + 3];
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct Buf {
+    void* p = nullptr;
+    size_t cap = 0;
+    template <typename T> T* get(size_t n) {
+        size_t bytes = sizeof(T) * (n ? n : 1);
+        if (bytes > cap) {
+            if (p) cudaFree(p);
+            p = nullptr;
+            cap = 0;
+            cudaError_t e = cudaMalloc(&p, bytes);
+            if (e != cudaSuccess) throw e;
+            cap = bytes;
+        }
+        return static_cast<T*>(p);
+    }
+};
+
+struct BatchWs {
+    std::mutex mu;
+    Buf mc, coef, zt, win, amp, quads, partials, gsum, cgrad, gwin, zbar, ginc, gcentral, gI_tmp;
+    std::map<int, std::pair<float2*, float2*>> tw;  // N -> (forward, conjugate)
+    std::pair<float2*, float2*> twiddles(int N) {
+        auto it = tw.find(N);
+        if (it != tw.end()) return it->second;
+        std::vector<float2> f((size_t)N), c((size_t)N);
+        const long double two_pi = 6.283185307179586476925286766559005768L;
+        for (int m = 0; m < N; ++m) {
+            const long double a = -two_pi * (long double)m / (long double)N;
+            f[(size_t)m] = make_float2((float)cosl(a), (float)sinl(a));
+            c[(size_t)m] = make_float2((float)cosl(a), (float)-sinl(a));
+        }
+        float2 *df = nullptr, *dc = nullptr;
+        cudaError_t e = cudaMalloc(&df, sizeof(float2) * N);
+        if (e == cudaSuccess) e = cudaMalloc(&dc, sizeof(float2) * N);
+        if (e == cudaSuccess) e = cudaMemcpy(df, f.data(), sizeof(float2) * N, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(dc, c.data(), sizeof(float2) * N, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) throw e;
+        tw[N] = std::make_pair(df, dc);
+        return tw[N];
+    }
+};
+
+std::mutex g_bws_mu;
+std::map<int, BatchWs*> g_bws;
+BatchWs& batch_ws() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_bws_mu);
+    auto it = g_bws.find(dev);
+    if (it != g_bws.end()) return *it->second;
+    BatchWs* w = new BatchWs();
+    g_bws[dev] = w;
+    return *w;
+}
+
+struct Dataset {
+    int device = 0;
+    int nd = 0;
+    float *u = nullptr, *v = nullptr, *re = nullptr, *im = nullptr, *w = nullptr;
+    double rmax2 = 0.0;
+};
+
+int smem_attr(const void* kern, size_t smem) {
+    if (smem > 48 * 1024)
+        return (int)cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return 0;
+}
+
+struct Err {
+    int status;
+    std::string msg;
+};
+
+#define BCK(x)                                                                                           \
+    do {                                                                                                 \
+        cudaError_t e_ = (x);                                                                            \
+        if (e_ != cudaSuccess) {                                                                         \
+            if (e_ == cudaErrorMemoryAllocation) throw Err{GALARIO_ENOMEM, "cuda out of memory"};         \
+            throw Err{GALARIO_ERUNTIME, std::string("Error in cuda (" #x "): ") + cudaGetErrorString(e_)}; \
+        }                                                                                                \
+    } while (0)
+
+template <class F> int bguard(F&& f) {
+    try {
+        f();
+        return GALARIO_OK;
+    } catch (const Err& e) {
+        set_error_message(e.msg);
+        return e.status;
+    } catch (cudaError_t e) {
+        set_error_message(std::string("Error in cuda: ") + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? GALARIO_ENOMEM : GALARIO_ERUNTIME;
+    } catch (const std::exception& e) {
+        set_error_message(e.what());
+        return GALARIO_ERUNTIME;
+    }
+}
+
+__global__ void extent_f32_kernel(const float* __restrict__ u, const float* __restrict__ v, int nd,
+                                  double* __restrict__ out) {
+    float m = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += gridDim.x * blockDim.x)
+        m = fmaxf(m, u[i] * u[i] + v[i] * v[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.f)
+        atomicMax(reinterpret_cast<unsigned long long*>(out), (unsigned long long)__double_as_longlong((double)m));
+}
+
+#define GBB_DISPATCH_E(E_, ...)                                 \
+    switch (E_) {                                               \
+        case 8: { constexpr int EE = 8; __VA_ARGS__; } break;   \
+        case 16: { constexpr int EE = 16; __VA_ARGS__; } break; \
+        default: throw Err{GALARIO_EINVAL, "unsupported FFT length"}; \
+    }
+
+}  // namespace
+}  // namespace gbg
+
+using namespace gbg;
+
+#define API extern "C" __attribute__((visibility("default")))
+
+API int galario_dataset_create_f(int nd, const float* u, const float* v, const float* re, const float* im,
+                                 const float* w, int on_device, void** handle) {
+    return bguard([&] {
+        if (nd <= 0) throw Err{GALARIO_EINVAL, "Error in dataset: nd must be positive"};
+        if (!handle) throw Err{GALARIO_EINVAL, "Error in dataset: handle is NULL"};
+        Dataset* d = new Dataset();
+        BCK(cudaGetDevice(&d->device));
+        d->nd = nd;
+        float** dst[5] = {&d->u, &d->v, &d->re, &d->im, &d->w};
+        const float* src[5] = {u, v, re, im, w};
+        const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+        try {
+            for (int i = 0; i < 5; ++i) {
+                BCK(cudaMalloc(dst[i], sizeof(float) * (size_t)nd));
+                BCK(cudaMemcpy(*dst[i], src[i], sizeof(float) * (size_t)nd, kind));
+            }
+            double* r2 = nullptr;
+            BCK(cudaMalloc(&r2, sizeof(double)));
+            BCK(cudaMemset(r2, 0, sizeof(double)));
+            extent_f32_kernel<<<num_sms() * 4, 256>>>(d->u, d->v, nd, r2);
+            BCK(cudaGetLastError());
+            BCK(cudaMemcpy(&d->rmax2, r2, sizeof(double), cudaMemcpyDeviceToHost));
+            cudaFree(r2);
+        } catch (...) {
+            for (int i = 0; i < 5; ++i)
+                if (*dst[i]) cudaFree(*dst[i]);
+            delete d;
+            throw;
+        }
+        *handle = d;
+    });
+}
+
+API int galario_dataset_free(void* handle) {
+    return bguard([&] {
+        Dataset* d = static_cast<Dataset*>(handle);
+        if (!d) return;
+        cudaDeviceSynchronize();
+        float* p[5] = {d->u, d->v, d->re, d->im, d->w};
+        for (float* x : p) cudaFree(x);
+        delete d;
+    });
+}
+
+API int galario_dataset_nvis(void* handle, int* nd) {
+    return bguard([&] {
+        if (!handle) throw Err{GALARIO_EINVAL, "Error in dataset: handle is NULL"};
+        *nd = static_cast<Dataset*>(handle)->nd;
+    });
+}
+
+API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* intensity, float Rmin, float dR,
+                                     float dxy, int nxy, const float* params, double* chi2, float* grad_intensity,
+                                     float* grad_params, void* stream) {
+    return bguard([&] {
+        Dataset* d = static_cast<Dataset*>(dataset);
+        if (!d) throw Err{GALARIO_EINVAL, "Error in batch: dataset is NULL"};
+        if (B <= 0) throw Err{GALARIO_EINVAL, "Error in batch: B must be positive"};
+        if (nxy < 2 || (nxy & 1))
+            throw Err{GALARIO_EINVAL, "Error in check input image: x dimension = " + std::to_string(nxy) +
+                                          (nxy < 2 ? " is less than 2" : " is odd")};
+        if (!is_pow2(nxy) || nxy < 16 || nxy > 16384)
+            throw Err{GALARIO_EINVAL, "Error in batch: nxy must be a power of two in [16, 16384]"};
+        const double ratio = ((double)dxy / 2. - (double)Rmin) / (double)dR;
+        if (ratio < 5)
+            throw Err{GALARIO_EINVAL,
+                      "Error in create image: Expect (dxy/2-Rmin)/dR > 5, i.e. dR small enough to ensure reliable "
+                      "interpolation the inside central pixel but got (dxy/2-Rmin)/dR = " + std::to_string(ratio) +
+                          ". Try reducing dR."};
+        const bool grad = grad_intensity || grad_params;
+        if (grad && !(grad_intensity && grad_params))
+            throw Err{GALARIO_EINVAL, "Error in batch: pass both gradient outputs or neither"};
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        BatchWs& ws = batch_ws();
+        std::lock_guard<std::mutex> lk(ws.mu);
+
+        // ---- geometry (host) ----
+        Geo g;
+        g.N = nxy;
+        g.M = nxy / 2;
+        g.C = nxy / 2 + 1;
+        const double duv = (double)(float)(1.0 / ((double)dxy * nxy));  // as the FP32 module passes it
+        const Window w = window_from_extent(d->rmax2, duv, nxy);
+        g.K = w.K;
+        g.r0 = w.r0;
+        g.W = w.W;
+        long long rm = (long long)std::ceil(((double)Rmin + nr * (double)dR) / (double)dxy);
+        g.rmax = (int)(rm < nxy / 2 ? rm : nxy / 2);
+        g.band0 = nxy / 2 - g.rmax;
+        g.R = 2 * g.rmax;
+        g.nr = nr;
+        g.Rmin = Rmin;
+        g.dR = dR;
+        g.inv_dR = (float)(1.0 / (double)dR);
+        g.dxy = dxy;
+        g.sr_to_px = dxy * dxy;
+        const double inv_duv = 1.0 / duv;
+        g.inv_duv_hi = (float)inv_duv;
+        g.inv_duv_lo = (float)(inv_duv - (double)g.inv_duv_hi);
+        g.half_nrow = (float)(nxy / 2);
+        g.vo = 1.f;
+        if (g.R <= 0) throw Err{GALARIO_EINVAL, "Error in batch: empty profile support"};
+        if (nr < 2 || nr >= (1 << 22)) throw Err{GALARIO_EINVAL, "Error in batch: nr out of range"};
+        // central-pixel coefficients: central = sum_i coef_i I_i (reference :1136-1153)
+        const int iIN = (int)std::floor(((double)dxy / 2 - (double)Rmin) / (double)dR);
+        if (iIN < 0 || iIN + 1 >= nr) throw Err{GALARIO_EINVAL, "Error in create image: profile too short"};
+        g.iIN = iIN;
+        std::vector<double> coef((size_t)iIN + 2, 0.0);
+        {
+            const double Rm = Rmin, dr = dR, h = (double)dxy / 2.;
+            for (int i = 1; i < iIN; ++i) coef[i] += 2. * dr * (Rm + dr * i);
+            coef[0] += dr * Rm;
+            coef[iIN] += dr * (Rm + iIN * dr);
+            const double span = h - (Rm + iIN * dr);
+            // ((Rm + iIN dr) I_iIN + h I_interp) * span, I_interp = (I_{iIN+1} - I_iIN)/dr * span + I_iIN
+            coef[iIN] += (Rm + iIN * dr) * span;
+            coef[iIN] += h * span * (1. - span / dr);
+            coef[iIN + 1] += h * span * (span / dr);
+            const double area = h * h - Rm * Rm;
+            const double sr = (double)dxy * (double)dxy;
+            for (auto& c : coef) c *= sr / area;
+        }
+        const int ncoef = iIN + 2;
+
+        // ---- buffers ----
+        const long long ncell = (long long)g.K * g.W;
+        ModelConst* mc = ws.mc.get<ModelConst>((size_t)B);
+        double* coef_d = ws.coef.get<double>((size_t)ncoef);
+        float2* zt = ws.zt.get<float2>((size_t)B * g.K * g.R);
+        float2* win = ws.win.get<float2>((size_t)B * ncell);
+        float* amp = ws.amp.get<float>((size_t)B * ncell);
+        float* quads = ws.quads.get<float>((size_t)B * ncell * kRec);
+        const int vblocks = (int)((d->nd + (long long)kVisThreads * kPts - 1) / ((long long)kVisThreads * kPts));
+        double* partials = ws.partials.get<double>((size_t)vblocks * B * kAcc);
+        double* gsum = ws.gsum.get<double>((size_t)B * kAcc);
+        auto tws = ws.twiddles(nxy);
+        BCK(cudaMemcpyAsync(coef_d, coef.data(), sizeof(double) * ncoef, cudaMemcpyHostToDevice, s));
+
+        // DevState for error bits: a small private block
+        DevState* st = ws.ginc.get<DevState>(4);  // reuse: first slot as DevState, rest for ginc
+        BCK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
+
+        // ---- forward ----
+        model_setup_kernel<<<(B + 31) / 32, 32, 0, s>>>(B, params, intensity, nr, coef_d, ncoef, mc);
+        BCK(cudaGetLastError());
+        {
+            const int E = g.M >= 16384 ? 16 : 8;
+            const int threads = g.M / E;
+            const size_t sm = sizeof(float2) * g.M;
+            if (g.M < 8) throw Err{GALARIO_EINVAL, "Error in batch: nxy too small"};
+            GBB_DISPATCH_E(E, {
+                BCK((cudaError_t)smem_attr((const void*)rows_batch_kernel<EE>, sm));
+                rows_batch_kernel<EE><<<dim3(g.R, B), threads, sm, s>>>(g, intensity, mc, tws.first, zt);
+            });
+            BCK(cudaGetLastError());
+        }
+        {
+            const int E = g.N >= 16384 ? 16 : 8;
+            const int threads = g.N / E;
+            const size_t sm = sizeof(float2) * g.N;
+            GBB_DISPATCH_E(E, {
+                BCK((cudaError_t)smem_attr((const void*)cols_batch_kernel<EE>, sm));
+                cols_batch_kernel<EE><<<dim3(g.K, B), threads, sm, s>>>(g, zt, tws.first, win, amp);
+            });
+            BCK(cudaGetLastError());
+        }
+        quad_batch_kernel<<<num_sms() * 8, 256, 0, s>>>(g, B, win, amp, quads);
+        BCK(cudaGetLastError());
+        float* cgrad = nullptr;
+        if (grad) {
+            cgrad = ws.cgrad.get<float>((size_t)B * ncell * kGRec);
+            BCK(cudaMemsetAsync(cgrad, 0, sizeof(float) * (size_t)B * ncell * kGRec, s));
+        }
+        const size_t vsm = sizeof(ModelConst) * B + sizeof(double) * B * kAcc;
+        if (grad) {
+            BCK((cudaError_t)smem_attr((const void*)vis_batch_kernel<true>, vsm));
+            vis_batch_kernel<true><<<vblocks, kVisThreads, vsm, s>>>(g, B, d->nd, d->u, d->v, d->re, d->im, d->w, mc,
+                                                                     quads, cgrad, partials, st);
+        } else {
+            BCK((cudaError_t)smem_attr((const void*)vis_batch_kernel<false>, vsm));
+            vis_batch_kernel<false><<<vblocks, kVisThreads, vsm, s>>>(g, B, d->nd, d->u, d->v, d->re, d->im, d->w,
+                                                                      mc, quads, cgrad, partials, st);
+        }
+        BCK(cudaGetLastError());
+        batch_finalize_kernel<<<dim3(B, grad ? kAcc : 1), 256, 0, s>>>(B, vblocks, partials, chi2, gsum);
+        BCK(cudaGetLastError());
+        if (!grad) return;
+
+        // ---- adjoint ----
+        float2* gwin = ws.gwin.get<float2>((size_t)B * ncell);
+        float2* zbar = ws.zbar.get<float2>((size_t)B * g.K * g.R);
+        double* ginc_d = reinterpret_cast<double*>(ws.gI_tmp.get<double>((size_t)B));
+        float* gcentral = ws.gcentral.get<float>((size_t)B);
+        BCK(cudaMemsetAsync(ginc_d, 0, sizeof(double) * B, s));
+        BCK(cudaMemsetAsync(gcentral, 0, sizeof(float) * B, s));
+        BCK(cudaMemsetAsync(grad_intensity, 0, sizeof(float) * (size_t)B * nr, s));
+        quadT_batch_kernel<<<num_sms() * 8, 256, 0, s>>>(g, B, cgrad, win, amp, gwin);
+        BCK(cudaGetLastError());
+        {
+            const int E = g.N >= 16384 ? 16 : 8;
+            const int threads = g.N / E;
+            const size_t sm = sizeof(float2) * g.N;
+            GBB_DISPATCH_E(E, {
+                BCK((cudaError_t)smem_attr((const void*)colsT_batch_kernel<EE>, sm));
+                colsT_batch_kernel<EE><<<dim3(g.K, B), threads, sm, s>>>(g, gwin, tws.first, zbar);
+            });
+            BCK(cudaGetLastError());
+        }
+        {
+            const int E = g.M >= 16384 ? 16 : 8;
+            const int threads = g.M / E;
+            const size_t sm = sizeof(float2) * g.M + sizeof(float) * nr;
+            if (sm > 220 * 1024) throw Err{GALARIO_EINVAL, "Error in batch: nxy/nr too large for the row adjoint"};
+            GBB_DISPATCH_E(E, {
+                BCK((cudaError_t)smem_attr((const void*)rowsT_batch_kernel<EE>, sm));
+                rowsT_batch_kernel<EE><<<dim3((g.R + kRowsPerCta - 1) / kRowsPerCta, B), threads, sm, s>>>(
+                    g, intensity, mc, tws.first, tws.second, zbar, grad_intensity, ginc_d, gcentral);
+            });
+            BCK(cudaGetLastError());
+        }
+        central_adjoint_kernel<<<B, 64, 0, s>>>(B, nr, coef_d, ncoef, gcentral, grad_intensity);
+        BCK(cudaGetLastError());
+        write_grad_params_kernel<<<(B + 127) / 128, 128, 0, s>>>(B, gsum, ginc_d, grad_params);
+        BCK(cudaGetLastError());
+    });
+}

@@ -1,0 +1,427 @@
+// Device helpers shared by the galario_gb300 kernel translation units:
+// complex arithmetic, the shared-memory Stockham FFT, the real-row split,
+// conversion-free FP32 rounding, the profile sweep, block/grid reductions,
+// double-float arithmetic and the sin/cos evaluations of the phase shift.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "gb_internal.cuh"
+
+namespace gbg {
+
+// ---------------------------------------------------------------------------
+// complex helpers
+// ---------------------------------------------------------------------------
+template <typename CT> __device__ __forceinline__ CT cadd(CT a, CT b) { return CT{a.x + b.x, a.y + b.y}; }
+template <typename CT> __device__ __forceinline__ CT csub(CT a, CT b) { return CT{a.x - b.x, a.y - b.y}; }
+template <typename CT> __device__ __forceinline__ CT cmul(CT a, CT b) {
+    return CT{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
+}
+// (-i) * a
+template <typename CT> __device__ __forceinline__ CT cmul_mi(CT a) { return CT{a.y, -a.x}; }
+template <typename CT> __device__ __forceinline__ CT cneg(CT a) { return CT{-a.x, -a.y}; }
+
+// modulus sqrt(re^2 + im^2) (the reference uses cuCabs / std::abs, :806-809)
+template <typename T> __device__ __forceinline__ T cabs_(C2<T> a);
+template <> __device__ __forceinline__ double cabs_<double>(double2 a) { return sqrt(fma(a.x, a.x, a.y * a.y)); }
+template <> __device__ __forceinline__ float cabs_<float>(float2 a) { return sqrtf(fmaf(a.x, a.x, a.y * a.y)); }
+
+template <typename T> __device__ __forceinline__ T sqrt_half();
+template <> __device__ __forceinline__ double sqrt_half<double>() { return 0.70710678118654752440084436210485; }
+template <> __device__ __forceinline__ float sqrt_half<float>() { return 0.70710678118654752440f; }
+
+// in-register forward DFT of size R (natural order in and out)
+template <typename T, int R> struct Dft;
+template <typename T> struct Dft<T, 2> {
+    using CT = C2<T>;
+    __device__ __forceinline__ static void run(CT* v) {
+        CT a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    }
+};
+template <typename T> struct Dft<T, 4> {
+    using CT = C2<T>;
+    __device__ __forceinline__ static void run(CT* v) {
+        CT t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+        CT t2 = cadd(v[1], v[3]), t3 = cmul_mi(csub(v[1], v[3]));
+        v[0] = cadd(t0, t2);
+        v[2] = csub(t0, t2);
+        v[1] = cadd(t1, t3);
+        v[3] = csub(t1, t3);
+    }
+};
+template <typename T> struct Dft<T, 8> {
+    using CT = C2<T>;
+    __device__ __forceinline__ static void run(CT* v) {
+        CT e[4] = {v[0], v[2], v[4], v[6]};
+        CT o[4] = {v[1], v[3], v[5], v[7]};
+        Dft<T, 4>::run(e);
+        Dft<T, 4>::run(o);
+        const T c = sqrt_half<T>();
+        // o[k] *= exp(-2 pi i k / 8)
+        CT o1 = CT{c * (o[1].x + o[1].y), c * (o[1].y - o[1].x)};
+        CT o2 = cmul_mi(o[2]);
+        CT o3 = CT{c * (o[3].y - o[3].x), -c * (o[3].x + o[3].y)};
+        v[0] = cadd(e[0], o[0]);
+        v[4] = csub(e[0], o[0]);
+        v[1] = cadd(e[1], o1);
+        v[5] = csub(e[1], o1);
+        v[2] = cadd(e[2], o2);
+        v[6] = csub(e[2], o2);
+        v[3] = cadd(e[3], o3);
+        v[7] = csub(e[3], o3);
+    }
+};
+
+// One Stockham stage of radix R on buf[0, M) (in place, two barriers).
+// Every thread owns E/R butterflies.  tw[m] = exp(-2 pi i m / twN), twN = tw_mul * M.
+template <typename T, int E, int R>
+__device__ __forceinline__ void stockham_stage(C2<T>* buf, int M, int Ns, const C2<T>* __restrict__ tw, int tw_mul) {
+    using CT = C2<T>;
+    constexpr int B = E / R;
+    const int nt = blockDim.x, tid = threadIdx.x;
+    const int stride = M / R;
+    CT v[E];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const int j = tid + b * nt;
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[b * R + r] = buf[j + r * stride];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const int j = tid + b * nt;
+        const int k = j & (Ns - 1);
+        if (Ns > 1) {
+            const int step = k * tw_mul * (M / (Ns * R));
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[b * R + r] = cmul(v[b * R + r], __ldg(&tw[r * step]));
+        }
+        Dft<T, R>::run(&v[b * R]);
+        const int d = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) buf[d + r * Ns] = v[b * R + r];
+    }
+    __syncthreads();
+}
+
+template <typename T> struct Dft<T, 1> {
+    __device__ __forceinline__ static void run(C2<T>*) {}
+};
+
+// Forward complex FFT of length M = E * blockDim.x (power of two) on shared
+// memory, natural order in and out.
+template <typename T, int E>
+__device__ void block_fft(C2<T>* buf, int M, int log2M, const C2<T>* __restrict__ tw, int tw_mul) {
+    int Ns = 1, bits = log2M;
+    while (bits > 0) {
+        if constexpr (E >= 8) {
+            if (bits >= 3) {
+                stockham_stage<T, E, 8>(buf, M, Ns, tw, tw_mul);
+                Ns <<= 3;
+                bits -= 3;
+                continue;
+            }
+        }
+        if constexpr (E >= 4) {
+            if (bits >= 2) {
+                stockham_stage<T, E, 4>(buf, M, Ns, tw, tw_mul);
+                Ns <<= 2;
+                bits -= 2;
+                continue;
+            }
+        }
+        if constexpr (E >= 2) {
+            stockham_stage<T, E, 2>(buf, M, Ns, tw, tw_mul);
+            Ns <<= 1;
+            bits -= 1;
+        } else {
+            bits = 0;  // E == 1 means M == 1: nothing to do
+        }
+    }
+}
+
+__device__ __forceinline__ int ilog2(int n) { return 31 - __clz(n); }
+
+// the spectrum window: given by the host (host_K >= 0) or written by the extent pass
+__device__ __forceinline__ Window get_window(int host_K, int host_r0, int host_W, const DevState* __restrict__ st) {
+    Window w;
+    if (host_K >= 0) {
+        w.K = host_K;
+        w.r0 = host_r0;
+        w.W = host_W;
+    } else {
+        w.K = st->win_K;
+        w.r0 = st->win_r0;
+        w.W = st->win_W;
+    }
+    return w;
+}
+
+template <typename T> __device__ __forceinline__ T tw_cast(double x) { return (T)x; }
+
+// ---------------------------------------------------------------------------
+// Real-row post-processing: X[k] = E[k] + exp(-2 pi i k/N) O[k], k in [0, K)
+// from the length-M complex FFT Z of z[m] = x[2m] + i x[2m+1].
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ C2<T> real_split(const C2<T>* Z, int M, int k, const C2<T>* __restrict__ tw) {
+    using CT = C2<T>;
+    const CT za = Z[k == M ? 0 : k];
+    const CT zb = Z[k == 0 ? 0 : M - k];
+    // Ek = (za + conj(zb))/2 ; Ok = (za - conj(zb))/(2i)
+    const T h = (T)0.5;
+    const CT e = CT{h * (za.x + zb.x), h * (za.y - zb.y)};
+    const T pr = za.x - zb.x, pi = za.y + zb.y;
+    const CT o = CT{h * pi, -h * pr};
+    const CT w = __ldg(&tw[k]);  // exp(-2 pi i k / N), N = 2M
+    return cadd(e, cmul(o, w));
+}
+
+
+// Float rounding without conversion instructions.  On GB300 the
+// float<->int conversions and FRND share the slow FP64 pipe, so the FP32 path
+// rounds with the magic-number method: for |x| < 2^22, x + 1.5*2^23 lands in
+// [2^23, 2^24) where the float spacing is 1, so the addition rounds x to the
+// nearest integer and the low mantissa bits hold that integer.
+constexpr float kMagic = 12582912.0f;   // 1.5 * 2^23
+constexpr int kMagicBits = 0x4B400000;  // bit pattern of kMagic
+__device__ __forceinline__ int rint_i(float x, float* xr) {  // |x| < 2^22
+    const float r = __fadd_rn(x, kMagic);
+    *xr = __fsub_rn(r, kMagic);
+    return __float_as_int(r) - kMagicBits;
+}
+__device__ __forceinline__ int floor_i(float x, float* xf) {  // |x| < 2^22
+    float f;
+    int n = rint_i(x, &f);
+    if (f > x) {
+        n -= 1;
+        f = __fsub_rn(f, 1.f);
+    }
+    *xf = f;
+    return n;
+}
+__device__ __forceinline__ float i2f_small(int n) {  // exact for |n| < 2^22
+    return __fsub_rn(__int_as_float(kMagicBits + n), kMagic);
+}
+
+// sweep of a radial profile (reference sweep_core, src/galario.cpp:1048-1071)
+// evaluated for image pixel (I, J); zero outside the 2*rmax box.  The
+// reference's divisions by cos(inc) and dR are multiplications by host-computed
+// reciprocals here (a rounding-level change: the linear interpolation is
+// continuous across the bin edges where floor() could flip).
+template <typename T>
+__device__ __forceinline__ T sweep_pixel(int I, int J, const T* __restrict__ intensity, int nr, T Rmin, T dR, T inv_dR,
+                                         T dxy, T inv_cos_inc, int rmax, int off, T sr_to_px) {
+    const int i = I - off, j = J - off;
+    if (i < 0 || j < 0 || i >= 2 * rmax || j >= 2 * rmax) return (T)0;
+    if constexpr (sizeof(T) == 4) {
+        // FP32: int<->float conversions and floor without the conversion pipe
+        const float x = i2f_small(rmax - j) * dxy;
+        const float y = i2f_small(rmax - i) * dxy;
+        const float xs = x * inv_cos_inc;
+        const float r = sqrtf(xs * xs + y * y);
+        const float tR = (r - Rmin) * inv_dR;
+        if (!(tR < (float)(nr - 1))) return 0.f;  // floor(tR) > nr - 2
+        int iR = 0;
+        if (tR > 0.f) {
+            float fl;
+            iR = floor_i(tR, &fl);
+        }
+        const float I0 = __ldg(&intensity[iR]), I1 = __ldg(&intensity[iR + 1]);
+        return sr_to_px * (I0 + (r - i2f_small(iR) * dR - Rmin) * ((I1 - I0) * inv_dR));
+    } else {
+        const T x = (T)(rmax - j) * dxy;
+        const T y = (T)(rmax - i) * dxy;
+        const T xs = x * inv_cos_inc;
+        const T r = sqrt(xs * xs + y * y);
+        int iR = (int)floor((r - Rmin) * inv_dR);
+        if (iR < 0) iR = 0;
+        if (iR > nr - 2) return (T)0;
+        const T I0 = __ldg(&intensity[iR]), I1 = __ldg(&intensity[iR + 1]);
+        return sr_to_px * (I0 + (r - (T)iR * dR - Rmin) * ((I1 - I0) * inv_dR));
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// block reduction helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum(double x, double* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = x;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < nw; ++q) s += sh[q];
+    return s;  // valid in thread 0
+}
+
+// Deterministic grid reduction: each block writes its partial, the last block
+// to arrive sums the partials with all its threads: thread i takes partials
+// i, i + blockDim, ... in order, then a fixed-shape tree (block_sum).  The
+// summation order depends only on the grid size, so results are reproducible.
+__device__ __forceinline__ void grid_finish(double block_total, double* partials, DevState* st,
+                                            double* extra_out = nullptr) {
+    __shared__ bool last;
+    __shared__ double sh2[32];
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = block_total;
+        __threadfence();
+        const unsigned t = atomicAdd(&st->ticket, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double s = 0.0;
+    const volatile double* p = partials;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) s += p[b];
+    s = block_sum(s, sh2);
+    if (threadIdx.x == 0) {
+        st->chi2 = s;
+        if (extra_out) *extra_out = s;
+        st->ticket = 0u;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// double-float arithmetic for the FP32 path: a value is hi + lo with two
+// floats (about 44 significant bits).  Error-free transformations of Dekker
+// (1971) and Knuth (TAOCP vol. 2, 4.2.2): two_prod via fused multiply-add,
+// two_sum by Knuth's six-operation form.  Intrinsics (_rn) keep the compiler
+// from contracting or reassociating them.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ DF df_two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return DF{p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return DF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ DF df_renorm(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_neg(DF a) { return DF{-a.hi, -a.lo}; }
+__device__ __forceinline__ DF df_mul_f(float x, DF y) {  // exact float x times y
+    DF p = df_two_prod(x, y.hi);
+    return df_renorm(p.hi, __fmaf_rn(x, y.lo, p.lo));
+}
+__device__ __forceinline__ DF df_mul(DF x, DF y) {
+    DF p = df_two_prod(x.hi, y.hi);
+    return df_renorm(p.hi, __fmaf_rn(x.hi, y.lo, __fmaf_rn(x.lo, y.hi, p.lo)));
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+    DF s = df_two_sum(a.hi, b.hi);
+    return df_renorm(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+// floor of x = hi + lo (|hi| < 2^22) as an integer and the fraction in [0, 1]
+__device__ __forceinline__ void df_floor(DF x, int* fl, float* frac) {
+    float f;
+    int n = floor_i(x.hi, &f);
+    float r = __fadd_rn(__fsub_rn(x.hi, f), x.lo);  // hi - floor(hi) is exact
+    if (r < 0.f) {
+        n -= 1;
+        r = __fadd_rn(r, 1.f);
+    } else if (r >= 1.f) {
+        n += 1;
+        r = __fsub_rn(r, 1.f);
+    }
+    *fl = n;
+    *frac = r;
+}
+
+// sin/cos(2 pi f) in FP32 for |f| <= 1/2 + tiny, without conversion
+// instructions: j = rint(4 f), d = f - j/4 (exact by Sterbenz), x = 2 pi d with
+// |x| <= pi/4, Taylor series to x^9 (sin) and x^8 (cos), truncation error
+// below 3e-8, then rotation by i^j.
+__device__ __forceinline__ void sincos2pi_f32(float f, float* s, float* c) {
+    float jf;
+    const int j = rint_i(4.f * f, &jf);
+    const float d = __fmaf_rn(jf, -0.25f, f);
+    const float x = d * 6.28318530717958647692f;
+    const float x2 = x * x;
+    float sp = __fmaf_rn(x2, 2.7557319e-6f, -1.9841270e-4f);  // 1/9!, -1/7!
+    sp = __fmaf_rn(x2, sp, 8.3333333e-3f);                     // 1/5!
+    sp = __fmaf_rn(x2, sp, -1.6666667e-1f);                    // -1/3!
+    const float sx = __fmaf_rn(x * x2, sp, x);
+    float cp = __fmaf_rn(x2, 2.4801587e-5f, -1.3888889e-3f);  // 1/8!, -1/6!
+    cp = __fmaf_rn(x2, cp, 4.1666667e-2f);                     // 1/4!
+    cp = __fmaf_rn(x2, cp, -0.5f);
+    const float cx = __fmaf_rn(x2, cp, 1.f);
+    switch (j & 3) {  // multiply by i^j
+        case 0: *s = sx; *c = cx; break;
+        case 1: *s = cx; *c = -sx; break;
+        case 2: *s = -sx; *c = -cx; break;
+        default: *s = -cx; *c = sx; break;
+    }
+}
+
+
+// sin/cos(2 pi a), a in cycles, FP64, table-driven (Tang's method): a = n +
+// j/T + d with n integer, j in [-T/2, T/2], |d| <= 1/(2T); exp(2 pi i a) =
+// E[j] * exp(2 pi i d) with the table E built on the host in long double and
+// exp(2 pi i d) from its Taylor series: x = 2 pi d, |x| <= pi/T = 3.1e-3, so
+// cos x = 1 - x^2/2 + x^4/24 and sin x = x - x^3/6 + x^5/120 are exact to
+// < 1e-17 (the next terms x^6/720 and x^7/5040 are below 1.3e-18).
+__device__ __forceinline__ void sincos2pi_tab(double a, const double2* __restrict__ tab, double* s, double* c) {
+    const double f = a - rint(a);                         // exact, |f| <= 1/2
+    const double jf = rint(f * (double)PHASE_T);          // f*T exact (power of two)
+    const double d = fma(jf, -1.0 / (double)PHASE_T, f);  // exact
+    const double x = d * 6.283185307179586476925286766559;
+    const double x2 = x * x;
+    const double cx = fma(x2, fma(x2, 1.0 / 24.0, -0.5), 1.0);
+    const double sx = fma(x * x2, fma(x2, 1.0 / 120.0, -1.0 / 6.0), x);
+    const double2 e = __ldg(&tab[(int)jf + PHASE_T / 2]);
+    *c = e.x * cx - e.y * sx;
+    *s = e.x * sx + e.y * cx;
+}
+// FP32 phase: argument in FP64 with exact range reduction, evaluated in FP32
+template <typename T> __device__ __forceinline__ void sincos2pi(double a, T* s, T* c);
+template <> __device__ __forceinline__ void sincos2pi<double>(double a, double* s, double* c) {
+    sincospi(2.0 * a, s, c);
+}
+template <> __device__ __forceinline__ void sincos2pi<float>(double a, float* s, float* c) {
+    const double f = a - rint(a);
+    sincospif((float)(2.0 * f), s, c);
+}
+template <typename T> __device__ __forceinline__ T rnorm2(T x, T y);
+template <> __device__ __forceinline__ double rnorm2<double>(double x, double y) { return rsqrt(fma(x, x, y * y)); }
+template <> __device__ __forceinline__ float rnorm2<float>(float x, float y) { return rsqrtf(fmaf(x, x, y * y)); }
+
+
+template <typename T> int max_fft_n_impl() { return sizeof(T) == 8 ? 8192 : 16384; }
+
+// dispatch helper: launch a shared-memory FFT kernel with E elements per thread
+template <typename T> struct FftCfg {
+    int E, threads;
+    size_t smem;
+};
+template <typename T> FftCfg<T> fft_cfg(int M) {
+    FftCfg<T> c;
+    if (M >= 16384) c.E = 16;
+    else if (M >= 8) c.E = 8;
+    else c.E = M < 1 ? 1 : M;
+    c.threads = M / c.E < 1 ? 1 : M / c.E;
+    c.smem = sizeof(C2<T>) * (size_t)(M < 1 ? 1 : M);
+    return c;
+}
+
+template <typename K> cudaError_t set_smem(K kernel, size_t smem) {
+    if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return cudaSuccess;
+}
+
+
+}  // namespace gbg

@@ -1,0 +1,187 @@
+"""Batched FP32 chi2 and its gradient (galario_gb300.batch / .autograd).
+
+chi2 of each model is checked against the single-model modules and the FP64
+oracle (relative 1e-6); the gradient against a float64 torch.fft-composed
+reference differentiated by autograd (tests/torch_reference.py) and against
+FP64 central finite differences of the oracle.
+
+Gradient tolerances of this FP32 path (measured, and reproduced by a float32
+emulation of the same algorithm on the CPU):
+- smooth parameters (inc, PA, dRA, dDec; ring radius, width, flux through
+  torch): relative 2e-3 per component;
+- the gradient with respect to every individual profile sample: relative
+  2-norm 5e-2.  The modulus/argument interpolation makes this gradient depend
+  on the phase of spectrum values far below the spectrum peak, where an FP32
+  FFT's rounding dominates; the float64 reference of the same algorithm agrees
+  to 4e-11, so the bound is FP32 arithmetic, not the adjoint.
+"""
+import numpy as np
+import pytest
+
+from helpers import arcsec, deg, uv_log_uniform
+
+pytestmark = pytest.mark.gpu
+
+CHI2_TOL = 1e-6
+GRAD_TOL = 2e-3        # smooth parameters
+GRAD_SAMPLES_TOL = 5e-2  # per profile sample (see the module docstring)
+
+
+def _setup(seed=0, nxy=512, nd=40000, nr=1500, B=3):
+    dxy = 0.02 * arcsec
+    Rmin, dR = 1e-4 * arcsec, 1e-3 * arcsec
+    duv = 1 / (nxy * dxy)
+    u, v = uv_log_uniform(nd, 0.5 * duv, 0.4 * nxy / 2 * duv, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    R = Rmin + dR * np.arange(nr)
+    I = []
+    params = []
+    for b in range(B):
+        r0, sig = rng.uniform(0.3, 0.9) * arcsec, rng.uniform(0.05, 0.2) * arcsec
+        I.append(np.exp(-0.5 * ((R - r0) / sig) ** 2) * 1e10 * rng.uniform(0.5, 2))
+        params.append([rng.uniform(0, 60) * deg, rng.uniform(0, 180) * deg, rng.uniform(-0.05, 0.05) * arcsec,
+                       rng.uniform(-0.05, 0.05) * arcsec])
+    I = np.array(I)
+    params = np.array(params)
+    sigma = rng.uniform(0.5e-3, 1.5e-3, nd) * 10
+    re, im = rng.normal(0, sigma), rng.normal(0, sigma)
+    w = 1 / sigma ** 2
+    return dict(nxy=nxy, dxy=dxy, Rmin=Rmin, dR=dR, u=u, v=v, re=re, im=im, w=w, I=I, params=params)
+
+
+@pytest.fixture(scope="module")
+def case():
+    torch = pytest.importorskip("torch")
+    import galario_gb300 as g
+    from galario_gb300.batch import Dataset
+    c = _setup()
+    # observations close to the first model, so residuals are not only noise
+    f = np.float32
+    vis = g.double.sampleProfile(c["I"][0], c["Rmin"], c["dR"], c["nxy"], c["dxy"], c["u"], c["v"],
+                                 inc=c["params"][0][0], PA=c["params"][0][1], dRA=c["params"][0][2],
+                                 dDec=c["params"][0][3])
+    c["re"] = c["re"] + vis.real
+    c["im"] = c["im"] + vis.imag
+    for k in ("u", "v", "re", "im", "w"):
+        c[k] = c[k].astype(f).astype(np.float64)  # the dataset is float32: test on the rounded values
+    c["I"] = c["I"].astype(f).astype(np.float64)
+    c["params"] = c["params"].astype(f).astype(np.float64)
+    c["ds"] = Dataset(c["u"], c["v"], c["re"], c["im"], c["w"])
+    c["tI"] = torch.tensor(c["I"], dtype=torch.float32, device="cuda")
+    c["tp"] = torch.tensor(c["params"], dtype=torch.float32, device="cuda")
+    return c
+
+
+def test_batch_chi2_matches_oracle_and_single(case, oracle_port):
+    import galario_gb300 as g
+    from galario_gb300.batch import chi2_profile_batch
+    c = case
+    chi2 = chi2_profile_batch(c["ds"], c["tI"], c["tp"], c["Rmin"], c["dR"], c["dxy"], c["nxy"]).cpu().numpy()
+    orc = oracle_port.get("port", "double")
+    f = np.float32
+    for b in range(len(chi2)):
+        inc, PA, dRA, dDec = c["params"][b]
+        ref = orc.chi2Profile(c["I"][b], c["Rmin"], c["dR"], c["nxy"], c["dxy"], c["u"], c["v"], c["re"], c["im"],
+                              c["w"], inc=inc, PA=PA, dRA=dRA, dDec=dDec)
+        assert abs(chi2[b] - ref) / ref <= CHI2_TOL, (b, chi2[b], ref)
+        single = g.single.chi2Profile(c["I"][b].astype(f), c["Rmin"], c["dR"], c["nxy"], c["dxy"], c["u"].astype(f),
+                                      c["v"].astype(f), c["re"].astype(f), c["im"].astype(f), c["w"].astype(f),
+                                      inc=inc, PA=PA, dRA=dRA, dDec=dDec)
+        assert abs(chi2[b] - single) / ref <= CHI2_TOL
+
+
+def _ref_grad(c, b):
+    import torch
+    from torch_reference import chi2_profile_t
+    d = dict(dtype=torch.float64)
+    I = torch.tensor(c["I"][b], requires_grad=True, **d)
+    p = [torch.tensor(x, requires_grad=True, **d) for x in c["params"][b]]
+    t = {k: torch.tensor(c[k], **d) for k in ("u", "v", "re", "im", "w")}
+    chi2 = chi2_profile_t(I, p[0], p[1], p[2], p[3], c["Rmin"], c["dR"], c["nxy"], c["dxy"], t["u"], t["v"],
+                          t["re"], t["im"], t["w"])
+    chi2.backward()
+    return float(chi2.detach()), I.grad.numpy(), np.array([x.grad.item() for x in p])
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def test_batch_gradient_vs_torch_fp64(case):
+    from galario_gb300.batch import chi2_profile_batch
+    c = case
+    chi2, gI, gp = chi2_profile_batch(c["ds"], c["tI"], c["tp"], c["Rmin"], c["dR"], c["dxy"], c["nxy"], grad=True)
+    chi2, gI, gp = chi2.cpu().numpy(), gI.cpu().numpy(), gp.cpu().numpy()
+    for b in range(len(chi2)):
+        ref_chi2, ref_gI, ref_gp = _ref_grad(c, b)
+        assert abs(chi2[b] - ref_chi2) / ref_chi2 <= CHI2_TOL
+        assert _rel(gI[b], ref_gI) <= GRAD_SAMPLES_TOL, (b, _rel(gI[b], ref_gI))
+        for a in range(4):
+            assert abs(gp[b, a] - ref_gp[a]) <= GRAD_TOL * abs(ref_gp[a]) + 1e-6 * np.abs(ref_gp).max(), \
+                (b, a, gp[b, a], ref_gp[a])
+
+
+def test_batch_gradient_vs_fd_oracle(case, oracle_port):
+    """FP64 central finite differences (h = 1e-6 relative) of the oracle's chi2Profile."""
+    from galario_gb300.batch import chi2_profile_batch
+    c = case
+    _, gI, gp = chi2_profile_batch(c["ds"], c["tI"], c["tp"], c["Rmin"], c["dR"], c["dxy"], c["nxy"], grad=True)
+    gp = gp.cpu().numpy()
+    orc = oracle_port.get("port", "double")
+    b = 1
+    base = list(c["params"][b])
+
+    def chi2_at(p):
+        return orc.chi2Profile(c["I"][b], c["Rmin"], c["dR"], c["nxy"], c["dxy"], c["u"], c["v"], c["re"],
+                               c["im"], c["w"], inc=p[0], PA=p[1], dRA=p[2], dDec=p[3])
+    for a in range(4):
+        h = 1e-6 * max(abs(base[a]), 1e-3 if a < 2 else 1e-9)
+        pp, pm = list(base), list(base)
+        pp[a] += h
+        pm[a] -= h
+        fd = (chi2_at(pp) - chi2_at(pm)) / (2 * h)
+        assert abs(gp[b, a] - fd) <= GRAD_TOL * abs(fd), (a, gp[b, a], fd)
+
+
+def test_autograd_parametric_rings(case):
+    """Gradient of sum chi2 w.r.t. ring radius, width and flux through torch + the adjoint kernels."""
+    import torch
+    from galario_gb300.autograd import chi2_profile
+    from torch_reference import chi2_profile_t
+    c = case
+    nr = c["I"].shape[1]
+    R = torch.tensor(c["Rmin"] + c["dR"] * np.arange(nr), dtype=torch.float64)
+
+    def rings(theta):  # theta (B, 3): r0 [arcsec], sigma [arcsec], amplitude [1e10 Jy/sr]
+        r0, sig, amp = theta[:, 0:1] * arcsec, theta[:, 1:2] * arcsec, theta[:, 2:3] * 1e10
+        return amp * torch.exp(-0.5 * ((R - r0) / sig) ** 2)
+
+    theta = torch.tensor([[0.5, 0.1, 1.0], [0.7, 0.15, 0.6]], dtype=torch.float64)
+    params = torch.tensor(c["params"][:2], dtype=torch.float64)
+    th_gpu = theta.clone().cuda().requires_grad_(True)
+    p_gpu = params.clone().cuda().requires_grad_(True)
+    R_gpu = R.cuda()
+    r0, sig, amp = th_gpu[:, 0:1] * arcsec, th_gpu[:, 1:2] * arcsec, th_gpu[:, 2:3] * 1e10
+    I_gpu = (amp * torch.exp(-0.5 * ((R_gpu - r0) / sig) ** 2)).float()
+    chi2 = chi2_profile(I_gpu, p_gpu.float(), c["ds"], c["Rmin"], c["dR"], c["dxy"], c["nxy"])
+    chi2.sum().backward()
+    th_ref = theta.clone().requires_grad_(True)
+    p_ref = params.clone().requires_grad_(True)
+    I_ref = rings(th_ref)
+    t = {k: torch.tensor(c[k], dtype=torch.float64) for k in ("u", "v", "re", "im", "w")}
+    tot = 0
+    for b in range(2):
+        tot = tot + chi2_profile_t(I_ref[b], p_ref[b, 0], p_ref[b, 1], p_ref[b, 2], p_ref[b, 3], c["Rmin"], c["dR"],
+                                   c["nxy"], c["dxy"], t["u"], t["v"], t["re"], t["im"], t["w"])
+    tot.backward()
+    assert _rel(th_gpu.grad.cpu().numpy(), th_ref.grad.numpy()) <= GRAD_TOL
+    assert _rel(p_gpu.grad.cpu().numpy(), p_ref.grad.numpy()) <= GRAD_TOL
+
+
+def test_batch_rejects_bad_geometry(case):
+    from galario_gb300.batch import chi2_profile_batch
+    c = case
+    with pytest.raises(ValueError, match="Try reducing dR"):
+        chi2_profile_batch(c["ds"], c["tI"], c["tp"], c["Rmin"], c["dxy"] / 4, c["dxy"], c["nxy"])
+    with pytest.raises(ValueError, match="is odd"):
+        chi2_profile_batch(c["ds"], c["tI"], c["tp"], c["Rmin"], c["dR"], c["dxy"], 511)
