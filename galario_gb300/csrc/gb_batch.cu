@@ -25,6 +25,7 @@
 // Reference semantics followed: sweep_core src/galario.cpp:1048-1071, central
 // pixel :1136-1153, interpolate_core :749-815, apply_phase_sampled_core
 // :877-884, uv_rotate_core :955-960, reduce_chi2 :1504-1538.
+#include <cub/cub.cuh>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -315,8 +316,11 @@ __device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, co
 // Accumulators per model and block: chi2, dPA, dRA, dDec
 constexpr int kAcc = 4;
 
+// Grid: x = blocks of kVisThreads * kPts visibilities, y = groups of Bg
+// models.  The hardware issues the x blocks of one group before the next, so
+// the cell records of about Bg models are live in L2 at a time.
 template <bool GRAD>
-__global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, int nd, const float* __restrict__ u,
+__global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, int Bg, int nd, const float* __restrict__ u,
                                                                 const float* __restrict__ v,
                                                                 const float* __restrict__ re,
                                                                 const float* __restrict__ im,
@@ -326,11 +330,13 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
                                                                 float* __restrict__ cgrad, double* __restrict__ partials,
                                                                 DevState* st) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int b0 = blockIdx.y * Bg;
+    const int nb = min(Bg, B - b0);
     ModelConst* smc = reinterpret_cast<ModelConst*>(smem_raw);
-    double* sacc = reinterpret_cast<double*>(smc + B);  // [B][kAcc]
+    double* sacc = reinterpret_cast<double*>(smc + Bg);  // [Bg][kAcc]
     __shared__ float red[kAcc][kVisThreads / 32];
-    for (int i = threadIdx.x; i < B; i += blockDim.x) smc[i] = mc[i];
-    for (int i = threadIdx.x; i < B * kAcc; i += blockDim.x) sacc[i] = 0.0;
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) smc[i] = mc[b0 + i];
+    for (int i = threadIdx.x; i < Bg * kAcc; i += blockDim.x) sacc[i] = 0.0;
     // this thread's points
     float pu[kPts], pv[kPts], pre[kPts], pim[kPts], pw[kPts];
     const long long base = (long long)blockIdx.x * kVisThreads * kPts + threadIdx.x;
@@ -348,51 +354,90 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
     const long long ncell = (long long)g.K * g.W;
     unsigned err = 0u;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int b = 0; b < B; ++b) {
-        const ModelConst m = smc[b];
+    for (int bl = 0; bl < nb; ++bl) {
+        const int b = b0 + bl;
+        const ModelConst m = smc[bl];
         const float* qb = quads + (size_t)b * ncell * kRec;
         float acc[kAcc] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int j = 0; j < kPts; ++j) {
-            if (pw[j] == 0.f) continue;
+            const bool live = pw[j] != 0.f;  // w = 0: padding (or a zero-weight visibility)
             PointEval p;
-            eval_point(g, m, qb, pu[j], pv[j], p);
-            err |= p.err;
+            p.cell = -1;
+            p.V = make_float2(0.f, 0.f);
+            if (live) {
+                eval_point(g, m, qb, pu[j], pv[j], p);
+                err |= p.err;
+            }
             const float dr = p.V.x - pre[j], di = p.V.y - pim[j];
-            acc[0] += pw[j] * (dr * dr + di * di);
-            if (GRAD && p.cell >= 0) {
-                // dchi2/dV
-                const float gx = 2.f * pw[j] * dr, gy = 2.f * pw[j] * di;
-                // phase shift V = U P: dchi2/dphi = -Im(conj(G) V); phi = 2 pi (u dRA + v dDec)
-                const float dphi = -(gx * p.V.y - gy * p.V.x);
-                acc[2] += dphi * 6.28318530717958647692f * pu[j];
-                acc[3] += dphi * 6.28318530717958647692f * pv[j];
-                // G_U = G conj(P)
-                const float gux = gx * p.pc + gy * p.ps, guy = -gx * p.ps + gy * p.pc;
-                // U = A * (zr, su zi) / |z|
-                const float ex = p.zr * p.rn, ey = p.zi * p.rn;  // e = z/|z|
-                const float gA = gux * ex + guy * (p.su * ey);
-                // gradient w.r.t. e (undo the conjugation for u < 0)
-                const float gex = p.A * gux, gey = p.su * p.A * guy;
-                const float dot = ex * gex + ey * gey;
-                const float gzx = (gex - ex * dot) * p.rn, gzy = (gey - ey * dot) * p.rn;
-                const float t = p.t, q = p.q;
-                const float wgt[4] = {(1.f - t) * (1.f - q), t * (1.f - q), t * q, (1.f - t) * q};
-                float4* dst = reinterpret_cast<float4*>(cgrad + ((size_t)b * ncell + p.cell) * kGRec);
-                atomicAdd(dst, make_float4(wgt[0] * gzx, wgt[0] * gzy, wgt[1] * gzx, wgt[1] * gzy));
-                atomicAdd(dst + 1, make_float4(wgt[2] * gzx, wgt[2] * gzy, wgt[3] * gzx, wgt[3] * gzy));
-                atomicAdd(dst + 2, make_float4(wgt[0] * gA, wgt[1] * gA, wgt[2] * gA, wgt[3] * gA));
-                // position: q = |u'|/duv, t = N/2 + vo su v'/duv; du'/dPA = -v', dv'/dPA = u'
-                const float dzqx = (p.y[3].x - p.y[0].x) + t * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
-                const float dzqy = (p.y[3].y - p.y[0].y) + t * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
-                const float dztx = (p.y[1].x - p.y[0].x) + q * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
-                const float dzty = (p.y[1].y - p.y[0].y) + q * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
-                const float dAq = (p.am[3] - p.am[0]) + t * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
-                const float dAt = (p.am[1] - p.am[0]) + q * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
-                const float gq = gzx * dzqx + gzy * dzqy + gA * dAq;
-                const float gt = gzx * dztx + gzy * dzty + gA * dAt;
-                const float inv_duv = g.inv_duv_hi;
-                acc[1] += gq * (p.su * (-p.vr) * inv_duv) + gt * (g.vo * p.su * p.ur * inv_duv);
+            if (live) acc[0] += pw[j] * (dr * dr + di * di);
+            if (GRAD) {
+                float rec[12];
+                const bool has = live && p.cell >= 0;
+                if (has) {
+                    // dchi2/dV
+                    const float gx = 2.f * pw[j] * dr, gy = 2.f * pw[j] * di;
+                    // phase shift V = U P: dchi2/dphi = -Im(conj(G) V); phi = 2 pi (u dRA + v dDec)
+                    const float dphi = -(gx * p.V.y - gy * p.V.x);
+                    acc[2] += dphi * 6.28318530717958647692f * pu[j];
+                    acc[3] += dphi * 6.28318530717958647692f * pv[j];
+                    // G_U = G conj(P)
+                    const float gux = gx * p.pc + gy * p.ps, guy = -gx * p.ps + gy * p.pc;
+                    // U = A * (zr, su zi) / |z|
+                    const float ex = p.zr * p.rn, ey = p.zi * p.rn;  // e = z/|z|
+                    const float gA = gux * ex + guy * (p.su * ey);
+                    // gradient w.r.t. e (undo the conjugation for u < 0)
+                    const float gex = p.A * gux, gey = p.su * p.A * guy;
+                    const float dot = ex * gex + ey * gey;
+                    const float gzx = (gex - ex * dot) * p.rn, gzy = (gey - ey * dot) * p.rn;
+                    const float t = p.t, q = p.q;
+                    const float wgt[4] = {(1.f - t) * (1.f - q), t * (1.f - q), t * q, (1.f - t) * q};
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) {
+                        rec[2 * cc] = wgt[cc] * gzx;
+                        rec[2 * cc + 1] = wgt[cc] * gzy;
+                        rec[8 + cc] = wgt[cc] * gA;
+                    }
+                    // position: q = |u'|/duv, t = N/2 + vo su v'/duv; du'/dPA = -v', dv'/dPA = u'
+                    const float dzqx = (p.y[3].x - p.y[0].x) + t * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
+                    const float dzqy = (p.y[3].y - p.y[0].y) + t * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
+                    const float dztx = (p.y[1].x - p.y[0].x) + q * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
+                    const float dzty = (p.y[1].y - p.y[0].y) + q * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
+                    const float dAq = (p.am[3] - p.am[0]) + t * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
+                    const float dAt = (p.am[1] - p.am[0]) + q * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
+                    const float gq = gzx * dzqx + gzy * dzqy + gA * dAq;
+                    const float gt = gzx * dztx + gzy * dzty + gA * dAt;
+                    const float inv_duv = g.inv_duv_hi;
+                    acc[1] += gq * (p.su * (-p.vr) * inv_duv) + gt * (g.vo * p.su * p.ur * inv_duv);
+                } else {
+#pragma unroll
+                    for (int cc = 0; cc < 12; ++cc) rec[cc] = 0.f;
+                }
+                // Scatter into the cell record.  Lanes of a warp hold consecutive
+                // visibilities of the spatially sorted dataset, so near the uv
+                // centre many of them hit the same cell: runs of equal cells are
+                // reduced with shuffles first and one lane per run adds atomically.
+                const long long key = has ? p.cell : -1 - (long long)lane;
+                const long long prev = __shfl_up_sync(0xffffffffu, key, 1);
+                const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || key != prev);
+                if (heads != 0xffffffffu) {
+                    const int seg = __popc(heads & ((2u << lane) - 1u));
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const int seg_d = __shfl_down_sync(0xffffffffu, seg, d);
+#pragma unroll
+                        for (int cc = 0; cc < 12; ++cc) {
+                            const float o = __shfl_down_sync(0xffffffffu, rec[cc], d);
+                            if (lane + d < 32 && seg_d == seg) rec[cc] += o;
+                        }
+                    }
+                }
+                if (has && ((heads >> lane) & 1u)) {
+                    float4* dst = reinterpret_cast<float4*>(cgrad + ((size_t)b * ncell + p.cell) * kGRec);
+                    atomicAdd(dst, make_float4(rec[0], rec[1], rec[2], rec[3]));
+                    atomicAdd(dst + 1, make_float4(rec[4], rec[5], rec[6], rec[7]));
+                    atomicAdd(dst + 2, make_float4(rec[8], rec[9], rec[10], rec[11]));
+                }
             }
         }
         // block reduction of this model's accumulators
@@ -407,13 +452,13 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
         if (threadIdx.x < (GRAD ? kAcc : 1)) {
             double s = 0.0;
             for (int q = 0; q < kVisThreads / 32; ++q) s += (double)red[threadIdx.x][q];
-            sacc[b * kAcc + threadIdx.x] = s;
+            sacc[bl * kAcc + threadIdx.x] = s;
         }
         __syncthreads();
     }
     if (err) atomicOr(&st->err, err);
-    double* dst = partials + (size_t)blockIdx.x * B * kAcc;
-    for (int i = threadIdx.x; i < B * kAcc; i += blockDim.x) dst[i] = sacc[i];
+    double* dst = partials + ((size_t)blockIdx.x * B + b0) * kAcc;
+    for (int i = threadIdx.x; i < nb * kAcc; i += blockDim.x) dst[i] = sacc[i];
 }
 
 // partials [blocks][B][kAcc] -> out[b][a] (fixed summation order)
@@ -727,6 +772,41 @@ __global__ void extent_f32_kernel(const float* __restrict__ u, const float* __re
         atomicMax(reinterpret_cast<unsigned long long*>(out), (unsigned long long)__double_as_longlong((double)m));
 }
 
+// Morton (Z-order) key of (u, v) on a 2^15 x 2^15 grid over [-rmax, rmax]^2:
+// visibilities close in the uv plane get close keys, for every rotation.
+__device__ __forceinline__ unsigned spread15(unsigned x) {
+    x &= 0x7fffu;
+    x = (x | (x << 8)) & 0x00ff00ffu;
+    x = (x | (x << 4)) & 0x0f0f0f0fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    x = (x | (x << 1)) & 0x55555555u;
+    return x;
+}
+__global__ void morton_kernel(const float* __restrict__ u, const float* __restrict__ v, int nd, float inv_span,
+                              unsigned* __restrict__ key, int* __restrict__ idx) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += gridDim.x * blockDim.x) {
+        float fu = (u[i] * inv_span + 0.5f) * 32767.f, fv = (v[i] * inv_span + 0.5f) * 32767.f;
+        fu = fminf(fmaxf(fu, 0.f), 32767.f);
+        fv = fminf(fmaxf(fv, 0.f), 32767.f);
+        key[i] = (spread15((unsigned)fu) << 1) | spread15((unsigned)fv);
+        idx[i] = i;
+    }
+}
+__global__ void gather5_kernel(const int* __restrict__ idx, int nd, const float* __restrict__ a0,
+                               const float* __restrict__ a1, const float* __restrict__ a2,
+                               const float* __restrict__ a3, const float* __restrict__ a4, float* __restrict__ b0,
+                               float* __restrict__ b1, float* __restrict__ b2, float* __restrict__ b3,
+                               float* __restrict__ b4) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += gridDim.x * blockDim.x) {
+        const int j = idx[i];
+        b0[i] = a0[j];
+        b1[i] = a1[j];
+        b2[i] = a2[j];
+        b3[i] = a3[j];
+        b4[i] = a4[j];
+    }
+}
+
 #define GBB_DISPATCH_E(E_, ...)                                 \
     switch (E_) {                                               \
         case 8: { constexpr int EE = 8; __VA_ARGS__; } break;   \
@@ -764,6 +844,40 @@ API int galario_dataset_create_f(int nd, const float* u, const float* v, const f
             BCK(cudaGetLastError());
             BCK(cudaMemcpy(&d->rmax2, r2, sizeof(double), cudaMemcpyDeviceToHost));
             cudaFree(r2);
+            // spatial order (chi2 is a sum: the order changes only the rounding)
+            if (d->rmax2 > 0.0 && std::isfinite(d->rmax2)) {
+                unsigned *k0 = nullptr, *k1 = nullptr;
+                int *i0 = nullptr, *i1 = nullptr;
+                float* tmp[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+                void* cub_tmp = nullptr;
+                size_t cub_bytes = 0;
+                auto cleanup = [&] {
+                    cudaFree(k0); cudaFree(k1); cudaFree(i0); cudaFree(i1); cudaFree(cub_tmp);
+                    for (float* t : tmp) cudaFree(t);
+                };
+                try {
+                    BCK(cudaMalloc(&k0, sizeof(unsigned) * nd));
+                    BCK(cudaMalloc(&k1, sizeof(unsigned) * nd));
+                    BCK(cudaMalloc(&i0, sizeof(int) * nd));
+                    BCK(cudaMalloc(&i1, sizeof(int) * nd));
+                    const float inv_span = (float)(0.5 / (std::sqrt(d->rmax2) * 1.0000001));
+                    morton_kernel<<<num_sms() * 4, 256>>>(d->u, d->v, nd, inv_span, k0, i0);
+                    BCK(cudaGetLastError());
+                    BCK(cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, k0, k1, i0, i1, nd, 0, 30));
+                    BCK(cudaMalloc(&cub_tmp, cub_bytes));
+                    BCK(cub::DeviceRadixSort::SortPairs(cub_tmp, cub_bytes, k0, k1, i0, i1, nd, 0, 30));
+                    for (int i = 0; i < 5; ++i) BCK(cudaMalloc(&tmp[i], sizeof(float) * nd));
+                    gather5_kernel<<<num_sms() * 4, 256>>>(i1, nd, d->u, d->v, d->re, d->im, d->w, tmp[0], tmp[1],
+                                                          tmp[2], tmp[3], tmp[4]);
+                    BCK(cudaGetLastError());
+                    BCK(cudaDeviceSynchronize());
+                    for (int i = 0; i < 5; ++i) std::swap(*dst[i], tmp[i]);
+                } catch (...) {
+                    cleanup();
+                    throw;
+                }
+                cleanup();
+            }
         } catch (...) {
             for (int i = 0; i < 5; ++i)
                 if (*dst[i]) cudaFree(*dst[i]);
@@ -914,15 +1028,21 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
             cgrad = ws.cgrad.get<float>((size_t)B * ncell * kGRec);
             BCK(cudaMemsetAsync(cgrad, 0, sizeof(float) * (size_t)B * ncell * kGRec, s));
         }
-        const size_t vsm = sizeof(ModelConst) * B + sizeof(double) * B * kAcc;
+        // models per group: the group's cell records (forward + gradient) within ~64 MiB of L2
+        const double rec_bytes = (double)ncell * (kRec + (grad ? kGRec : 0)) * sizeof(float);
+        int Bg = (int)std::floor(64.0 * 1024 * 1024 / rec_bytes);
+        if (Bg < 1) Bg = 1;
+        if (Bg > B) Bg = B;
+        const int ngroups = (B + Bg - 1) / Bg;
+        const size_t vsm = sizeof(ModelConst) * Bg + sizeof(double) * Bg * kAcc;
         if (grad) {
             BCK((cudaError_t)smem_attr((const void*)vis_batch_kernel<true>, vsm));
-            vis_batch_kernel<true><<<vblocks, kVisThreads, vsm, s>>>(g, B, d->nd, d->u, d->v, d->re, d->im, d->w, mc,
-                                                                     quads, cgrad, partials, st);
+            vis_batch_kernel<true><<<dim3(vblocks, ngroups), kVisThreads, vsm, s>>>(
+                g, B, Bg, d->nd, d->u, d->v, d->re, d->im, d->w, mc, quads, cgrad, partials, st);
         } else {
             BCK((cudaError_t)smem_attr((const void*)vis_batch_kernel<false>, vsm));
-            vis_batch_kernel<false><<<vblocks, kVisThreads, vsm, s>>>(g, B, d->nd, d->u, d->v, d->re, d->im, d->w,
-                                                                      mc, quads, cgrad, partials, st);
+            vis_batch_kernel<false><<<dim3(vblocks, ngroups), kVisThreads, vsm, s>>>(
+                g, B, Bg, d->nd, d->u, d->v, d->re, d->im, d->w, mc, quads, cgrad, partials, st);
         }
         BCK(cudaGetLastError());
         batch_finalize_kernel<<<dim3(B, grad ? kAcc : 1), 256, 0, s>>>(B, vblocks, partials, chi2, gsum);
