@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -44,20 +45,19 @@ void set_error_message(const std::string& msg);  // gb_api.cu
 
 namespace {
 
-constexpr int kPts = 4;        // visibilities per thread in the vis pass
 constexpr int kVisThreads = 256;
 constexpr int kRowsPerCta = 4;  // image rows per CTA in the row adjoint
 constexpr int kRec = 16;        // floats per forward cell record (QUAD_REC)
 constexpr int kGRec = 12;       // floats per gradient cell record
 
 struct ModelConst {
-    DF cpa, spa;          // cos / sin PA
-    DF dra, ddec;         // rotated offsets (radians)
+    DF cu, sv;            // cos(PA) / duv, sin(PA) / duv: (u, v) -> rotated grid coordinates
+    DF dra, ddec;         // offsets (radians); the phase u'dRA' + v'dDec' = u dRA + v dDec
     float inv_cos_inc;    // 1 / cos(inc)
     float tan_inc;        // tan(inc)
     float central;        // central pixel value (Jy/pixel)
-    int rotate, phase;
-    float pad[3];
+    int phase;
+    float pad[4];
 };
 
 struct Geo {  // geometry shared by all models of a batch
@@ -71,7 +71,8 @@ struct Geo {  // geometry shared by all models of a batch
 // forward kernels
 // ---------------------------------------------------------------------------
 __global__ void model_setup_kernel(int B, const float* __restrict__ params, const float* __restrict__ intensity,
-                                   int nr, const double* __restrict__ central_coef, int ncoef, ModelConst* mc) {
+                                   int nr, const double* __restrict__ central_coef, int ncoef, double inv_duv,
+                                   ModelConst* mc) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
     const double inc = params[4 * b + 0], PA = params[4 * b + 1];
@@ -83,15 +84,12 @@ __global__ void model_setup_kernel(int B, const float* __restrict__ params, cons
         r.lo = (float)(x - (double)r.hi);
         return r;
     };
-    const double c = cos(PA), s = sin(PA);
-    m.rotate = (PA != 0.0);
-    m.cpa = split(m.rotate ? c : 1.0);
-    m.spa = split(m.rotate ? s : 0.0);
-    const double dra = m.rotate ? dRA * c - dDec * s : dRA;
-    const double ddec = m.rotate ? dRA * s + dDec * c : dDec;
-    m.dra = split(dra);
-    m.ddec = split(ddec);
-    m.phase = !(dra == 0.0 && ddec == 0.0);
+    const double c = (PA != 0.0) ? cos(PA) : 1.0, s = (PA != 0.0) ? sin(PA) : 0.0;
+    m.cu = split(c * inv_duv);
+    m.sv = split(s * inv_duv);
+    m.dra = split(dRA);
+    m.ddec = split(dDec);
+    m.phase = !(dRA == 0.0 && dDec == 0.0);
     const double ci = cos(inc);
     m.inv_cos_inc = (float)(1.0 / ci);
     m.tan_inc = (float)tan(inc);
@@ -99,7 +97,7 @@ __global__ void model_setup_kernel(int B, const float* __restrict__ params, cons
     const float* I = intensity + (size_t)b * nr;
     for (int i = 0; i < ncoef; ++i) cen += central_coef[i] * (double)I[i];
     m.central = (float)cen;
-    m.pad[0] = m.pad[1] = m.pad[2] = 0.f;
+    m.pad[0] = m.pad[1] = m.pad[2] = m.pad[3] = 0.f;
     mc[b] = m;
 }
 
@@ -232,20 +230,15 @@ __device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, co
         p.err = ERR_UV_NONFINITE;
         return;
     }
-    DF ur = DF{u, 0.f}, vr = DF{v, 0.f};
-    if (m.rotate) {
-        ur = df_add(df_mul_f(u, m.cpa), df_neg(df_mul_f(v, m.spa)));
-        vr = df_add(df_mul_f(u, m.spa), df_mul_f(v, m.cpa));
-    }
-    p.ur = ur.hi;
-    p.vr = vr.hi;
-    const float su = copysignf(1.f, ur.hi);
+    // rotated coordinates in grid units, double-float: a = u'/duv, c = v'/duv
+    const DF a = df_add(df_mul_f(u, m.cu), df_neg(df_mul_f(v, m.sv)));
+    const DF cv = df_add(df_mul_f(u, m.sv), df_mul_f(v, m.cu));
+    p.ur = a.hi;
+    p.vr = cv.hi;
+    const float su = copysignf(1.f, a.hi);
     p.su = su;
-    const DF inv_duv = DF{g.inv_duv_hi, g.inv_duv_lo};
-    const DF au = ur.hi < 0.f ? df_neg(ur) : ur;
-    const DF indu = df_mul(au, inv_duv);
-    const DF sv = (g.vo * su < 0.f) ? df_neg(vr) : vr;
-    const DF indv = df_add(DF{g.half_nrow, 0.f}, df_mul(sv, inv_duv));
+    const DF indu = a.hi < 0.f ? df_neg(a) : a;
+    const DF indv = df_add(DF{g.half_nrow, 0.f}, (g.vo * su < 0.f) ? df_neg(cv) : cv);
     const float lim = 8.f * g.half_nrow;
     if (!(indu.hi < lim && indv.hi > -lim && indv.hi < lim)) {
         p.err = ERR_UV_OUTSIDE;
@@ -302,7 +295,8 @@ __device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, co
     p.pc = 1.f;
     p.ps = 0.f;
     if (m.phase) {
-        const DF ph = df_add(df_mul(ur, m.dra), df_mul(vr, m.ddec));
+        // u'dRA' + v'dDec' = u dRA + v dDec (both pairs rotated by PA)
+        const DF ph = df_add(df_mul_f(u, m.dra), df_mul_f(v, m.ddec));
         float n;
         if (fabsf(ph.hi) < 4194304.f) rint_i(ph.hi, &n);
         else n = rintf(ph.hi);
@@ -316,10 +310,10 @@ __device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, co
 // Accumulators per model and block: chi2, dPA, dRA, dDec
 constexpr int kAcc = 4;
 
-// Grid: x = blocks of kVisThreads * kPts visibilities, y = groups of Bg
+// Grid: x = blocks of kVisThreads * PTS visibilities, y = groups of Bg
 // models.  The hardware issues the x blocks of one group before the next, so
 // the cell records of about Bg models are live in L2 at a time.
-template <bool GRAD>
+template <bool GRAD, int PTS>
 __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, int Bg, int nd, const float* __restrict__ u,
                                                                 const float* __restrict__ v,
                                                                 const float* __restrict__ re,
@@ -338,10 +332,10 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
     for (int i = threadIdx.x; i < nb; i += blockDim.x) smc[i] = mc[b0 + i];
     for (int i = threadIdx.x; i < Bg * kAcc; i += blockDim.x) sacc[i] = 0.0;
     // this thread's points
-    float pu[kPts], pv[kPts], pre[kPts], pim[kPts], pw[kPts];
-    const long long base = (long long)blockIdx.x * kVisThreads * kPts + threadIdx.x;
+    float pu[PTS], pv[PTS], pre[PTS], pim[PTS], pw[PTS];
+    const long long base = (long long)blockIdx.x * kVisThreads * PTS + threadIdx.x;
 #pragma unroll
-    for (int j = 0; j < kPts; ++j) {
+    for (int j = 0; j < PTS; ++j) {
         const long long i = base + (long long)j * kVisThreads;
         const bool in = i < nd;
         pu[j] = in ? __ldg(&u[i]) : 0.f;
@@ -360,7 +354,7 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
         const float* qb = quads + (size_t)b * ncell * kRec;
         float acc[kAcc] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int j = 0; j < kPts; ++j) {
+        for (int j = 0; j < PTS; ++j) {
             const bool live = pw[j] != 0.f;  // w = 0: padding (or a zero-weight visibility)
             PointEval p;
             p.cell = -1;
@@ -398,7 +392,8 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
                         rec[2 * cc + 1] = wgt[cc] * gzy;
                         rec[8 + cc] = wgt[cc] * gA;
                     }
-                    // position: q = |u'|/duv, t = N/2 + vo su v'/duv; du'/dPA = -v', dv'/dPA = u'
+                    // position: q = |a|, t = N/2 + vo su c with a = u'/duv, c = v'/duv;
+                    // da/dPA = -c, dc/dPA = a
                     const float dzqx = (p.y[3].x - p.y[0].x) + t * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
                     const float dzqy = (p.y[3].y - p.y[0].y) + t * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
                     const float dztx = (p.y[1].x - p.y[0].x) + q * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
@@ -407,8 +402,7 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
                     const float dAt = (p.am[1] - p.am[0]) + q * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
                     const float gq = gzx * dzqx + gzy * dzqy + gA * dAq;
                     const float gt = gzx * dztx + gzy * dzty + gA * dAt;
-                    const float inv_duv = g.inv_duv_hi;
-                    acc[1] += gq * (p.su * (-p.vr) * inv_duv) + gt * (g.vo * p.su * p.ur * inv_duv);
+                    acc[1] += gq * (p.su * (-p.vr)) + gt * (g.vo * p.su * p.ur);
                 } else {
 #pragma unroll
                     for (int cc = 0; cc < 12; ++cc) rec[cc] = 0.f;
@@ -563,7 +557,7 @@ __global__ void __launch_bounds__(1024) rowsT_batch_kernel(Geo g, const float* _
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* buf = reinterpret_cast<float2*>(smem_raw);           // M complex
     float* gIs = reinterpret_cast<float*>(buf + g.M);            // nr floats
-    __shared__ double shd[32];
+    __shared__ double sinc;
     __shared__ int lo_bin, hi_bin;
     const int b = blockIdx.y;
     const ModelConst m = mc[b];
@@ -573,8 +567,10 @@ __global__ void __launch_bounds__(1024) rowsT_batch_kernel(Geo g, const float* _
     if (threadIdx.x == 0) {
         lo_bin = g.nr;
         hi_bin = -1;
+        sinc = 0.0;
     }
     float ginc_acc = 0.f;
+    int my_lo = g.nr, my_hi = -1;  // bins this thread touched
     const int off = g.N / 2 - g.rmax;
     const int M = g.M;
     for (int rr = 0; rr < kRowsPerCta; ++rr) {
@@ -627,20 +623,23 @@ __global__ void __launch_bounds__(1024) rowsT_batch_kernel(Geo g, const float* _
             const float gxs = xb * g.sr_to_px;
             atomicAdd(&gIs[iR], gxs * (1.f - frac));
             atomicAdd(&gIs[iR + 1], gxs * frac);
-            atomicMin(&lo_bin, iR);
-            atomicMax(&hi_bin, iR + 1);
+            my_lo = min(my_lo, iR);
+            my_hi = max(my_hi, iR + 1);
             if (r > 0.f) {
                 const float slope = (__ldg(&Ib[iR + 1]) - __ldg(&Ib[iR])) * g.inv_dR;
                 ginc_acc += gxs * slope * (xs * xs * m.tan_inc) / r;  // dr/dinc = xs^2 tan(inc) / r
             }
         }
     }
+    // once per thread (the block may be narrower than a warp for small images)
+    atomicMin(&lo_bin, my_lo);
+    atomicMax(&hi_bin, my_hi);
+    atomicAdd(&sinc, (double)ginc_acc);
     __syncthreads();
     float* gIb = gI + (size_t)b * g.nr;
     for (int i = lo_bin + threadIdx.x; i <= hi_bin; i += blockDim.x)
         if (gIs[i] != 0.f) atomicAdd(&gIb[i], gIs[i]);
-    const double tot = block_sum((double)ginc_acc, shd);
-    if (threadIdx.x == 0) atomicAdd(&ginc[b], tot);
+    if (threadIdx.x == 0) atomicAdd(&ginc[b], sinc);
 }
 
 // adjoint of the central pixel: I_bar += coef * x_bar(center)
@@ -663,6 +662,71 @@ __global__ void write_grad_params_kernel(int B, const double* __restrict__ gsum,
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
+// launch-shape autotuner: per geometry, each pass's candidate shapes (complex
+// values per thread of the FFT passes, visibilities per thread of the vis pass)
+// are timed once with CUDA events on the caller's stream and the fastest is
+// cached.  GALARIO_AUTOTUNE=0 keeps the default shapes.
+// ---------------------------------------------------------------------------
+struct Shape {
+    int e_rows, e_cols, e_colsT, e_rowsT, pts;
+};
+struct TuneKey {
+    int N, K, W, R, B, nd, grad, nr;
+    bool operator<(const TuneKey& o) const {
+        return std::memcmp(this, &o, sizeof(TuneKey)) < 0;
+    }
+};
+std::vector<int> fft_candidates(int L) {
+    std::vector<int> c;
+    for (int e : {8, 16})
+        if (L / e >= 1 && L / e <= 1024 && L % e == 0) c.push_back(e);
+    return c;
+}
+Shape default_shape(const Geo& g) {
+    Shape sh;
+    sh.e_rows = g.M >= 16384 ? 16 : 8;
+    sh.e_cols = g.N >= 16384 ? 16 : 8;
+    sh.e_colsT = sh.e_cols;
+    sh.e_rowsT = sh.e_rows;
+    sh.pts = 4;
+    return sh;
+}
+bool autotune_enabled() {
+    const char* v = std::getenv("GALARIO_AUTOTUNE");
+    return !(v && v[0] == '0');
+}
+struct Tuner {
+    cudaStream_t s;
+    cudaEvent_t a = nullptr, b = nullptr;
+    explicit Tuner(cudaStream_t st) : s(st) {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+    }
+    ~Tuner() {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+    template <class F> int best(const std::vector<int>& cand, F&& run) {
+        int best_c = cand.empty() ? 8 : cand[0];
+        float best_ms = 1e30f;
+        for (int c : cand) {
+            run(c);  // warm-up
+            cudaEventRecord(a, s);
+            run(c);
+            cudaEventRecord(b, s);
+            if (cudaEventSynchronize(b) != cudaSuccess) break;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_c = c;
+            }
+        }
+        return best_c;
+    }
+};
+
 struct Buf {
     void* p = nullptr;
     size_t cap = 0;
@@ -682,7 +746,8 @@ struct Buf {
 
 struct BatchWs {
     std::mutex mu;
-    Buf mc, coef, zt, win, amp, quads, partials, gsum, cgrad, gwin, zbar, ginc, gcentral, gI_tmp;
+    Buf mc, coef, zt, win, amp, quads, partials, gsum, cgrad, gwin, zbar, ginc, gcentral, gI_tmp, state;
+    std::map<TuneKey, Shape> shapes;
     std::map<int, std::pair<float2*, float2*>> tw;  // N -> (forward, conjugate)
     std::pair<float2*, float2*> twiddles(int N) {
         auto it = tw.find(N);
@@ -987,100 +1052,136 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
         float2* win = ws.win.get<float2>((size_t)B * ncell);
         float* amp = ws.amp.get<float>((size_t)B * ncell);
         float* quads = ws.quads.get<float>((size_t)B * ncell * kRec);
-        const int vblocks = (int)((d->nd + (long long)kVisThreads * kPts - 1) / ((long long)kVisThreads * kPts));
-        double* partials = ws.partials.get<double>((size_t)vblocks * B * kAcc);
+        const int max_vblocks = (int)((d->nd + (long long)kVisThreads * 2 - 1) / ((long long)kVisThreads * 2));
+        double* partials = ws.partials.get<double>((size_t)max_vblocks * B * kAcc);
         double* gsum = ws.gsum.get<double>((size_t)B * kAcc);
         auto tws = ws.twiddles(nxy);
         BCK(cudaMemcpyAsync(coef_d, coef.data(), sizeof(double) * ncoef, cudaMemcpyHostToDevice, s));
-
-        // DevState for error bits: a small private block
-        DevState* st = ws.ginc.get<DevState>(4);  // reuse: first slot as DevState, rest for ginc
+        DevState* st = ws.state.get<DevState>(1);
         BCK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
-
-        // ---- forward ----
-        model_setup_kernel<<<(B + 31) / 32, 32, 0, s>>>(B, params, intensity, nr, coef_d, ncoef, mc);
-        BCK(cudaGetLastError());
-        {
-            const int E = g.M >= 16384 ? 16 : 8;
-            const int threads = g.M / E;
-            const size_t sm = sizeof(float2) * g.M;
-            if (g.M < 8) throw Err{GALARIO_EINVAL, "Error in batch: nxy too small"};
-            GBB_DISPATCH_E(E, {
-                BCK((cudaError_t)smem_attr((const void*)rows_batch_kernel<EE>, sm));
-                rows_batch_kernel<EE><<<dim3(g.R, B), threads, sm, s>>>(g, intensity, mc, tws.first, zt);
-            });
-            BCK(cudaGetLastError());
-        }
-        {
-            const int E = g.N >= 16384 ? 16 : 8;
-            const int threads = g.N / E;
-            const size_t sm = sizeof(float2) * g.N;
-            GBB_DISPATCH_E(E, {
-                BCK((cudaError_t)smem_attr((const void*)cols_batch_kernel<EE>, sm));
-                cols_batch_kernel<EE><<<dim3(g.K, B), threads, sm, s>>>(g, zt, tws.first, win, amp);
-            });
-            BCK(cudaGetLastError());
-        }
-        quad_batch_kernel<<<num_sms() * 8, 256, 0, s>>>(g, B, win, amp, quads);
-        BCK(cudaGetLastError());
-        float* cgrad = nullptr;
-        if (grad) {
-            cgrad = ws.cgrad.get<float>((size_t)B * ncell * kGRec);
-            BCK(cudaMemsetAsync(cgrad, 0, sizeof(float) * (size_t)B * ncell * kGRec, s));
-        }
-        // models per group: the group's cell records (forward + gradient) within ~64 MiB of L2
+        float* cgrad = grad ? ws.cgrad.get<float>((size_t)B * ncell * kGRec) : nullptr;
+        float2* gwin = grad ? ws.gwin.get<float2>((size_t)B * ncell) : nullptr;
+        float2* zbar = grad ? ws.zbar.get<float2>((size_t)B * g.K * g.R) : nullptr;
+        double* ginc_d = grad ? ws.gI_tmp.get<double>((size_t)B) : nullptr;
+        float* gcentral = grad ? ws.gcentral.get<float>((size_t)B) : nullptr;
+        // models per group of the vis pass: the group's cell records within ~64 MiB of L2
         const double rec_bytes = (double)ncell * (kRec + (grad ? kGRec : 0)) * sizeof(float);
         int Bg = (int)std::floor(64.0 * 1024 * 1024 / rec_bytes);
         if (Bg < 1) Bg = 1;
         if (Bg > B) Bg = B;
         const int ngroups = (B + Bg - 1) / Bg;
-        const size_t vsm = sizeof(ModelConst) * Bg + sizeof(double) * Bg * kAcc;
-        if (grad) {
-            BCK((cudaError_t)smem_attr((const void*)vis_batch_kernel<true>, vsm));
-            vis_batch_kernel<true><<<dim3(vblocks, ngroups), kVisThreads, vsm, s>>>(
-                g, B, Bg, d->nd, d->u, d->v, d->re, d->im, d->w, mc, quads, cgrad, partials, st);
-        } else {
-            BCK((cudaError_t)smem_attr((const void*)vis_batch_kernel<false>, vsm));
-            vis_batch_kernel<false><<<dim3(vblocks, ngroups), kVisThreads, vsm, s>>>(
-                g, B, Bg, d->nd, d->u, d->v, d->re, d->im, d->w, mc, quads, cgrad, partials, st);
+
+        // ---- launchers, one per pass, parameterised by the tuned shape ----
+        auto fft_threads = [](int L, int E) { return L / E; };
+        auto rows = [&](int E) {
+            const size_t sm = sizeof(float2) * g.M;
+            GBB_DISPATCH_E(E, {
+                BCK((cudaError_t)smem_attr((const void*)rows_batch_kernel<EE>, sm));
+                rows_batch_kernel<EE><<<dim3(g.R, B), fft_threads(g.M, EE), sm, s>>>(g, intensity, mc, tws.first, zt);
+            });
+            BCK(cudaGetLastError());
+        };
+        auto cols = [&](int E) {
+            const size_t sm = sizeof(float2) * g.N;
+            GBB_DISPATCH_E(E, {
+                BCK((cudaError_t)smem_attr((const void*)cols_batch_kernel<EE>, sm));
+                cols_batch_kernel<EE><<<dim3(g.K, B), fft_threads(g.N, EE), sm, s>>>(g, zt, tws.first, win, amp);
+            });
+            BCK(cudaGetLastError());
+        };
+        auto vis = [&](int pts) {
+            const int vb = (int)((d->nd + (long long)kVisThreads * pts - 1) / ((long long)kVisThreads * pts));
+            const size_t vsm = sizeof(ModelConst) * Bg + sizeof(double) * Bg * kAcc;
+            const dim3 grid(vb, ngroups);
+#define GBB_VIS(G_, P_)                                                                                        \
+    do {                                                                                                       \
+        BCK((cudaError_t)smem_attr((const void*)vis_batch_kernel<G_, P_>, vsm));                               \
+        vis_batch_kernel<G_, P_><<<grid, kVisThreads, vsm, s>>>(g, B, Bg, d->nd, d->u, d->v, d->re, d->im,    \
+                                                               d->w, mc, quads, cgrad, partials, st);          \
+    } while (0)
+            if (grad) {
+                if (pts == 2) GBB_VIS(true, 2);
+                else GBB_VIS(true, 4);
+            } else {
+                if (pts == 2) GBB_VIS(false, 2);
+                else GBB_VIS(false, 4);
+            }
+#undef GBB_VIS
+            BCK(cudaGetLastError());
+            return vb;
+        };
+        auto colsT = [&](int E) {
+            const size_t sm = sizeof(float2) * g.N;
+            GBB_DISPATCH_E(E, {
+                BCK((cudaError_t)smem_attr((const void*)colsT_batch_kernel<EE>, sm));
+                colsT_batch_kernel<EE><<<dim3(g.K, B), fft_threads(g.N, EE), sm, s>>>(g, gwin, tws.first, zbar);
+            });
+            BCK(cudaGetLastError());
+        };
+        auto rowsT = [&](int E) {
+            const size_t sm = sizeof(float2) * g.M + sizeof(float) * nr;
+            if (sm > 220 * 1024) throw Err{GALARIO_EINVAL, "Error in batch: nxy/nr too large for the row adjoint"};
+            GBB_DISPATCH_E(E, {
+                BCK((cudaError_t)smem_attr((const void*)rowsT_batch_kernel<EE>, sm));
+                rowsT_batch_kernel<EE><<<dim3((g.R + kRowsPerCta - 1) / kRowsPerCta, B), fft_threads(g.M, EE), sm, s>>>(
+                    g, intensity, mc, tws.first, tws.second, zbar, grad_intensity, ginc_d, gcentral);
+            });
+            BCK(cudaGetLastError());
+        };
+        auto zero_grads = [&] {
+            BCK(cudaMemsetAsync(cgrad, 0, sizeof(float) * (size_t)B * ncell * kGRec, s));
+            BCK(cudaMemsetAsync(ginc_d, 0, sizeof(double) * B, s));
+            BCK(cudaMemsetAsync(gcentral, 0, sizeof(float) * B, s));
+            BCK(cudaMemsetAsync(grad_intensity, 0, sizeof(float) * (size_t)B * nr, s));
+        };
+
+        // ---- launch shapes: tuned once per geometry ----
+        Shape sh = default_shape(g);
+        const TuneKey key{g.N, g.K, g.W, g.R, B, d->nd, grad ? 1 : 0, nr};
+        auto it = ws.shapes.find(key);
+        if (it != ws.shapes.end()) {
+            sh = it->second;
+        } else if (autotune_enabled()) {
+            // valid inputs for every pass, then each candidate timed in isolation
+            model_setup_kernel<<<(B + 31) / 32, 32, 0, s>>>(B, params, intensity, nr, coef_d, ncoef, inv_duv, mc);
+            BCK(cudaGetLastError());
+            rows(sh.e_rows);
+            cols(sh.e_cols);
+            quad_batch_kernel<<<num_sms() * 8, 256, 0, s>>>(g, B, win, amp, quads);
+            BCK(cudaGetLastError());
+            if (grad) zero_grads();
+            Tuner tu(s);
+            sh.e_rows = tu.best(fft_candidates(g.M), [&](int e) { rows(e); });
+            sh.e_cols = tu.best(fft_candidates(g.N), [&](int e) { cols(e); });
+            sh.pts = tu.best({2, 4}, [&](int p) { vis(p); });
+            if (grad) {
+                quadT_batch_kernel<<<num_sms() * 8, 256, 0, s>>>(g, B, cgrad, win, amp, gwin);
+                BCK(cudaGetLastError());
+                sh.e_colsT = tu.best(fft_candidates(g.N), [&](int e) { colsT(e); });
+                sh.e_rowsT = tu.best(fft_candidates(g.M), [&](int e) { rowsT(e); });
+            }
+            ws.shapes[key] = sh;
+            BCK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
         }
+
+        // ---- forward ----
+        model_setup_kernel<<<(B + 31) / 32, 32, 0, s>>>(B, params, intensity, nr, coef_d, ncoef, inv_duv, mc);
         BCK(cudaGetLastError());
+        rows(sh.e_rows);
+        cols(sh.e_cols);
+        quad_batch_kernel<<<num_sms() * 8, 256, 0, s>>>(g, B, win, amp, quads);
+        BCK(cudaGetLastError());
+        if (grad) zero_grads();
+        const int vblocks = vis(sh.pts);
         batch_finalize_kernel<<<dim3(B, grad ? kAcc : 1), 256, 0, s>>>(B, vblocks, partials, chi2, gsum);
         BCK(cudaGetLastError());
         if (!grad) return;
 
         // ---- adjoint ----
-        float2* gwin = ws.gwin.get<float2>((size_t)B * ncell);
-        float2* zbar = ws.zbar.get<float2>((size_t)B * g.K * g.R);
-        double* ginc_d = reinterpret_cast<double*>(ws.gI_tmp.get<double>((size_t)B));
-        float* gcentral = ws.gcentral.get<float>((size_t)B);
-        BCK(cudaMemsetAsync(ginc_d, 0, sizeof(double) * B, s));
-        BCK(cudaMemsetAsync(gcentral, 0, sizeof(float) * B, s));
-        BCK(cudaMemsetAsync(grad_intensity, 0, sizeof(float) * (size_t)B * nr, s));
         quadT_batch_kernel<<<num_sms() * 8, 256, 0, s>>>(g, B, cgrad, win, amp, gwin);
         BCK(cudaGetLastError());
-        {
-            const int E = g.N >= 16384 ? 16 : 8;
-            const int threads = g.N / E;
-            const size_t sm = sizeof(float2) * g.N;
-            GBB_DISPATCH_E(E, {
-                BCK((cudaError_t)smem_attr((const void*)colsT_batch_kernel<EE>, sm));
-                colsT_batch_kernel<EE><<<dim3(g.K, B), threads, sm, s>>>(g, gwin, tws.first, zbar);
-            });
-            BCK(cudaGetLastError());
-        }
-        {
-            const int E = g.M >= 16384 ? 16 : 8;
-            const int threads = g.M / E;
-            const size_t sm = sizeof(float2) * g.M + sizeof(float) * nr;
-            if (sm > 220 * 1024) throw Err{GALARIO_EINVAL, "Error in batch: nxy/nr too large for the row adjoint"};
-            GBB_DISPATCH_E(E, {
-                BCK((cudaError_t)smem_attr((const void*)rowsT_batch_kernel<EE>, sm));
-                rowsT_batch_kernel<EE><<<dim3((g.R + kRowsPerCta - 1) / kRowsPerCta, B), threads, sm, s>>>(
-                    g, intensity, mc, tws.first, tws.second, zbar, grad_intensity, ginc_d, gcentral);
-            });
-            BCK(cudaGetLastError());
-        }
+        colsT(sh.e_colsT);
+        rowsT(sh.e_rowsT);
         central_adjoint_kernel<<<B, 64, 0, s>>>(B, nr, coef_d, ncoef, gcentral, grad_intensity);
         BCK(cudaGetLastError());
         write_grad_params_kernel<<<(B + 127) / 128, 128, 0, s>>>(B, gsum, ginc_d, grad_params);
