@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "../../include/galario_gb300.h"
+#include "gb_device.cuh"
 #include "gb_internal.cuh"
 
 namespace gbg {
@@ -113,7 +114,8 @@ struct Ctx {
     cudaStream_t stream = nullptr;
     DevBuf state, partials, img, prof, u, v, re, im, w, vis, zt, win, amp, quad, urot, vrot;
     double2* phase_tab = nullptr;  // table of the FP64 phase shift (PHASE_T + 1 entries)
-    std::map<std::pair<int, int>, void*> tw;  // (N, sizeof(T)) -> table
+    std::map<std::pair<int, int>, void*> tw;   // (N, sizeof(T)) -> table
+    std::map<std::pair<int, int>, void*> stw;  // (L, sizeof(T)) -> stage twiddles
     DevState* host_state = nullptr;           // pinned mirror of DevState
     // optional per-stage CUDA-event timing (galario_stage_timing)
     bool timing = false;
@@ -154,6 +156,20 @@ struct Ctx {
         for (DevBuf* b : bufs) b->release();
         for (auto& kv : tw) cudaFree(kv.second);
         tw.clear();
+        for (auto& kv : stw) cudaFree(kv.second);
+        stw.clear();
+    }
+    // stage twiddles of the shared-memory FFT of length L (power of two), cached per (L, precision)
+    template <typename T> const C2<T>* stage_tw(int L) {
+        auto key = std::make_pair(L, (int)sizeof(T));
+        auto it = stw.find(key);
+        if (it != stw.end()) return static_cast<const C2<T>*>(it->second);
+        std::vector<C2<T>> h = stage_twiddles<T>(L, fft_e<T>(L));
+        void* d = nullptr;
+        CK(cudaMalloc(&d, sizeof(C2<T>) * h.size()));
+        CK(cudaMemcpy(d, h.data(), sizeof(C2<T>) * h.size(), cudaMemcpyHostToDevice));
+        stw[key] = d;
+        return static_cast<const C2<T>*>(d);
     }
     // twiddles exp(-2 pi i m / N), m in [0, N), from long double, cached per (N, precision)
     template <typename T> const C2<T>* twiddles(int N) {
@@ -303,19 +319,21 @@ template <typename T> struct Pipe {
         double* partials = as<double>(c.partials, (size_t)L::vis_grid(nd > 0 ? nd : 1));
         if (!have_extent) timed(c, s, ST_EXTENT, [&] { CK(L::extent(u, v, nd, N, duv, st, s)); });
         int band0 = 0, band1 = N;
+        const CT* stw_rows = c.stage_tw<T>(N / 2 > 0 ? N / 2 : 1);
+        const CT* stw_cols = c.stage_tw<T>(N);
         if (img) {
-            timed(c, s, ST_ROWS, [&] { CK(L::rows_image(img, N, tw, zt, -1, st, duv, true, s)); });
+            timed(c, s, ST_ROWS, [&] { CK(L::rows_image(img, N, tw, stw_rows, zt, -1, st, duv, true, s)); });
         } else {
             band0 = N / 2 - pg->rmax;
             band1 = N / 2 + pg->rmax;
             timed(c, s, ST_ROWS, [&] {
-                CK(L::rows_profile(prof, nr, Rmin, dR, dxy, std::cos(inc), pg->rmax, pg->central, N, tw, zt, st,
-                                   duv, s));
+                CK(L::rows_profile(prof, nr, Rmin, dR, dxy, std::cos(inc), pg->rmax, pg->central, N, tw, stw_rows, zt,
+                                   st, duv, s));
             });
         }
         // window layout: column k at win + k*N, rows [r0, r0+W) contiguous
         timed(c, s, ST_COLS,
-              [&] { CK(L::cols(zt, N, band0, band1, tw, win, amp, 1, N, -1, -1, -1, st, duv, true, s)); });
+              [&] { CK(L::cols(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, -1, -1, -1, st, duv, true, s)); });
         timed(c, s, ST_QUAD, [&] { CK(L::quads(win, amp, 1, N, C, st, quads, qcap, -1, -1, -1, s)); });
         typename L::VisArgs a;
         a.spec = win;
@@ -661,8 +679,8 @@ template <typename T> struct Api {
         CK(cudaMemcpy2DAsync(img_d, sizeof(T) * N, data, sizeof(T) * 2 * C, sizeof(T) * N, N, cudaMemcpyHostToDevice,
                              s));
         const CT* tw = c.twiddles<T>(N);
-        CK(L::rows_image(img_d, N, tw, zt, C, st, 1.0, false, s));
-        CK(L::cols(zt, N, 0, N, tw, out, nullptr, C, 1, C, 0, N, st, 1.0, false, s));
+        CK(L::rows_image(img_d, N, tw, c.stage_tw<T>(N / 2), zt, C, st, 1.0, false, s));
+        CK(L::cols(zt, N, 0, N, tw, c.stage_tw<T>(N), out, nullptr, C, 1, C, 0, N, st, 1.0, false, s));
         d2h(data, out, sizeof(CT) * (size_t)N * C, s);
         CK(cudaStreamSynchronize(s));
     }

@@ -101,10 +101,11 @@ __global__ void model_setup_kernel(int B, const float* __restrict__ params, cons
     mc[b] = m;
 }
 
-template <int E>
-__global__ void __launch_bounds__(1024) rows_batch_kernel(Geo g, const float* __restrict__ intensity,
+template <int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) rows_batch_kernel(Geo g, const float* __restrict__ intensity,
                                                           const ModelConst* __restrict__ mc,
-                                                          const float2* __restrict__ tw, float2* __restrict__ zt) {
+                                                          const float2* __restrict__ tw,
+                                                          const float2* __restrict__ stw, float2* __restrict__ zt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* buf = reinterpret_cast<float2*>(smem_raw);
     const int b = blockIdx.y;
@@ -123,10 +124,10 @@ __global__ void __launch_bounds__(1024) rows_batch_kernel(Geo g, const float* __
             if (J0 == g.N / 2) a = m.central;
             if (J1 == g.N / 2) c = m.central;
         }
-        buf[mm] = make_float2(a, c);
+        buf[sp(mm)] = make_float2(a, c);
     }
     __syncthreads();
-    block_fft<float, E>(buf, g.M, ilog2(g.M), tw, 2);
+    block_fft<float, E>(buf, g.M, ilog2(g.M), stw);
     const float sgn = (I & 1) ? -1.f : 1.f;
     float2* out = zt + (size_t)b * g.K * g.R;
     for (int k = threadIdx.x; k < g.K; k += blockDim.x) {
@@ -135,9 +136,9 @@ __global__ void __launch_bounds__(1024) rows_batch_kernel(Geo g, const float* __
     }
 }
 
-template <int E>
-__global__ void __launch_bounds__(1024) cols_batch_kernel(Geo g, const float2* __restrict__ zt,
-                                                          const float2* __restrict__ tw, float2* __restrict__ win,
+template <int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) cols_batch_kernel(Geo g, const float2* __restrict__ zt,
+                                                          const float2* __restrict__ stw, float2* __restrict__ win,
                                                           float* __restrict__ amp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* buf = reinterpret_cast<float2*>(smem_raw);
@@ -145,16 +146,16 @@ __global__ void __launch_bounds__(1024) cols_batch_kernel(Geo g, const float2* _
     const float2* col = zt + ((size_t)b * g.K + k) * g.R;
     for (int i = threadIdx.x; i < g.N; i += blockDim.x) {
         const int q = i - g.band0;
-        buf[i] = (q >= 0 && q < g.R) ? __ldg(&col[q]) : make_float2(0.f, 0.f);
+        buf[sp(i)] = (q >= 0 && q < g.R) ? __ldg(&col[q]) : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    block_fft<float, E>(buf, g.N, ilog2(g.N), tw, 1);
+    block_fft<float, E>(buf, g.N, ilog2(g.N), stw);
     const int par = (k + g.N / 2) & 1;
     float2* wcol = win + ((size_t)b * g.K + k) * g.W;
     float* acol = amp + ((size_t)b * g.K + k) * g.W;
     for (int q = threadIdx.x; q < g.W; q += blockDim.x) {
         const int r = g.r0 + q;
-        float2 x = buf[r];
+        float2 x = buf[sp(r)];
         if ((r & 1) ^ par) x = make_float2(-x.x, -x.y);
         wcol[q] = x;
         acol[q] = sqrtf(fmaf(x.x, x.x, x.y * x.y));
@@ -520,9 +521,9 @@ __global__ void quadT_batch_kernel(Geo g, int B, const float* __restrict__ cgrad
 // adjoint of the column pass: inverse column FFT of the window gradient, kept
 // on the band rows.  IFFT(x) = conj(FFT(conj(x))): the forward transform runs
 // on the conjugated column.
-template <int E>
-__global__ void __launch_bounds__(1024) colsT_batch_kernel(Geo g, const float2* __restrict__ gwin,
-                                                           const float2* __restrict__ tw,
+template <int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) colsT_batch_kernel(Geo g, const float2* __restrict__ gwin,
+                                                           const float2* __restrict__ stw,
                                                            float2* __restrict__ zbar) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* buf = reinterpret_cast<float2*>(smem_raw);
@@ -531,13 +532,13 @@ __global__ void __launch_bounds__(1024) colsT_batch_kernel(Geo g, const float2* 
     for (int i = threadIdx.x; i < g.N; i += blockDim.x) {
         const int q = i - g.r0;
         const float2 x = (q >= 0 && q < g.W) ? col[q] : make_float2(0.f, 0.f);
-        buf[i] = make_float2(x.x, -x.y);
+        buf[sp(i)] = make_float2(x.x, -x.y);
     }
     __syncthreads();
-    block_fft<float, E>(buf, g.N, ilog2(g.N), tw, 1);
+    block_fft<float, E>(buf, g.N, ilog2(g.N), stw);
     float2* out = zbar + ((size_t)b * g.K + k) * g.R;
     for (int q = threadIdx.x; q < g.R; q += blockDim.x) {
-        const float2 x = buf[g.band0 + q];
+        const float2 x = buf[sp(g.band0 + q)];
         out[q] = make_float2(x.x, -x.y);
     }
 }
@@ -546,17 +547,17 @@ __global__ void __launch_bounds__(1024) colsT_batch_kernel(Geo g, const float2* 
 // (-1)^I Re(sum_{k<K} zbar[k] e^{+2 pi i j k/N}) via the half-length inverse
 // complex FFT (Hermitian weights), then the sweep adjoint into the profile
 // and the inclination.
-template <int E>
-__global__ void __launch_bounds__(1024) rowsT_batch_kernel(Geo g, const float* __restrict__ intensity,
+template <int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) rowsT_batch_kernel(Geo g, const float* __restrict__ intensity,
                                                            const ModelConst* __restrict__ mc,
-                                                           const float2* __restrict__ tw,
+                                                           const float2* __restrict__ stw,
                                                            const float2* __restrict__ twc,
                                                            const float2* __restrict__ zbar,
                                                            float* __restrict__ gI, double* __restrict__ ginc,
                                                            float* __restrict__ gcentral) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* buf = reinterpret_cast<float2*>(smem_raw);           // M complex
-    float* gIs = reinterpret_cast<float*>(buf + g.M);            // nr floats
+    float* gIs = reinterpret_cast<float*>(buf + fft_slots(g.M));  // nr floats
     __shared__ double sinc;
     __shared__ int lo_bin, hi_bin;
     const int b = blockIdx.y;
@@ -593,17 +594,17 @@ __global__ void __launch_bounds__(1024) rowsT_batch_kernel(Geo g, const float* _
             const float2 w = twc[k];  // e^{+2 pi i k / N}
             const float2 Op = make_float2(d.x * w.x - d.y * w.y, d.x * w.y + d.y * w.x);
             // Z = E' + i O', stored conjugated: the inverse FFT is conj(FFT(conj(Z)))
-            buf[k] = make_float2(Ep.x - Op.y, -(Ep.y + Op.x));
+            buf[sp(k)] = make_float2(Ep.x - Op.y, -(Ep.y + Op.x));
         }
         __syncthreads();
-        block_fft<float, E>(buf, M, ilog2(M), tw, 2);
+        block_fft<float, E>(buf, M, ilog2(M), stw);
         const float sgn = (I & 1) ? -1.f : 1.f;
         // sweep adjoint over the box pixels of this row
         const int i_box = I - off;
         const float y = i2f_small(g.rmax - i_box) * g.dxy;
         for (int j = threadIdx.x; j < 2 * g.rmax; j += blockDim.x) {
             const int J = j + off;
-            const float2 zz = buf[J >> 1];  // conj(z): x[2m] = Re z, x[2m+1] = Im z = -zz.y
+            const float2 zz = buf[sp(J >> 1)];  // conj(z): x[2m] = Re z, x[2m+1] = Im z = -zz.y
             const float xb = sgn * ((J & 1) ? -zz.y : zz.x);
             if (I == g.N / 2 && J == g.N / 2) {  // central pixel: its own adjoint
                 gcentral[b] = xb;
@@ -748,6 +749,19 @@ struct BatchWs {
     std::mutex mu;
     Buf mc, coef, zt, win, amp, quads, partials, gsum, cgrad, gwin, zbar, ginc, gcentral, gI_tmp, state;
     std::map<TuneKey, Shape> shapes;
+    std::map<std::pair<int, int>, float2*> stw;  // (L, E) -> stage twiddles
+    const float2* stage_tw(int L, int E) {
+        auto key = std::make_pair(L, E);
+        auto it = stw.find(key);
+        if (it != stw.end()) return it->second;
+        std::vector<float2> h = stage_twiddles<float>(L, E);
+        float2* d = nullptr;
+        cudaError_t e = cudaMalloc(&d, sizeof(float2) * h.size());
+        if (e == cudaSuccess) e = cudaMemcpy(d, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) throw e;
+        stw[key] = d;
+        return d;
+    }
     std::map<int, std::pair<float2*, float2*>> tw;  // N -> (forward, conjugate)
     std::pair<float2*, float2*> twiddles(int N) {
         auto it = tw.find(N);
@@ -872,11 +886,19 @@ __global__ void gather5_kernel(const int* __restrict__ idx, int nd, const float*
     }
 }
 
-#define GBB_DISPATCH_E(E_, ...)                                 \
-    switch (E_) {                                               \
-        case 8: { constexpr int EE = 8; __VA_ARGS__; } break;   \
-        case 16: { constexpr int EE = 16; __VA_ARGS__; } break; \
-        default: throw Err{GALARIO_EINVAL, "unsupported FFT length"}; \
+// (values per thread EE, block-size bound TT) for an FFT with `threads` threads
+#define GBB_CASE_T(E_V, THR, ...)                                                          \
+    {                                                                                      \
+        constexpr int EE = E_V;                                                            \
+        if ((THR) <= 256) { constexpr int TT = 256; __VA_ARGS__; }                         \
+        else if ((THR) <= 512) { constexpr int TT = 512; __VA_ARGS__; }                    \
+        else { constexpr int TT = 1024; __VA_ARGS__; }                                     \
+    }
+#define GBB_DISPATCH_E(E_, THR, ...)                                      \
+    switch (E_) {                                                         \
+        case 8: GBB_CASE_T(8, THR, __VA_ARGS__) break;                    \
+        case 16: GBB_CASE_T(16, THR, __VA_ARGS__) break;                  \
+        default: throw Err{GALARIO_EINVAL, "unsupported FFT length"};     \
     }
 
 }  // namespace
@@ -1074,18 +1096,20 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
         // ---- launchers, one per pass, parameterised by the tuned shape ----
         auto fft_threads = [](int L, int E) { return L / E; };
         auto rows = [&](int E) {
-            const size_t sm = sizeof(float2) * g.M;
-            GBB_DISPATCH_E(E, {
-                BCK((cudaError_t)smem_attr((const void*)rows_batch_kernel<EE>, sm));
-                rows_batch_kernel<EE><<<dim3(g.R, B), fft_threads(g.M, EE), sm, s>>>(g, intensity, mc, tws.first, zt);
+            const size_t sm = sizeof(float2) * fft_slots(g.M);
+            GBB_DISPATCH_E(E, fft_threads(g.M, E), {
+                BCK((cudaError_t)smem_attr((const void*)rows_batch_kernel<EE, TT>, sm));
+                rows_batch_kernel<EE, TT><<<dim3(g.R, B), fft_threads(g.M, EE), sm, s>>>(
+                    g, intensity, mc, tws.first, ws.stage_tw(g.M, EE), zt);
             });
             BCK(cudaGetLastError());
         };
         auto cols = [&](int E) {
-            const size_t sm = sizeof(float2) * g.N;
-            GBB_DISPATCH_E(E, {
-                BCK((cudaError_t)smem_attr((const void*)cols_batch_kernel<EE>, sm));
-                cols_batch_kernel<EE><<<dim3(g.K, B), fft_threads(g.N, EE), sm, s>>>(g, zt, tws.first, win, amp);
+            const size_t sm = sizeof(float2) * fft_slots(g.N);
+            GBB_DISPATCH_E(E, fft_threads(g.N, E), {
+                BCK((cudaError_t)smem_attr((const void*)cols_batch_kernel<EE, TT>, sm));
+                cols_batch_kernel<EE, TT><<<dim3(g.K, B), fft_threads(g.N, EE), sm, s>>>(
+                    g, zt, ws.stage_tw(g.N, EE), win, amp);
             });
             BCK(cudaGetLastError());
         };
@@ -1111,20 +1135,21 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
             return vb;
         };
         auto colsT = [&](int E) {
-            const size_t sm = sizeof(float2) * g.N;
-            GBB_DISPATCH_E(E, {
-                BCK((cudaError_t)smem_attr((const void*)colsT_batch_kernel<EE>, sm));
-                colsT_batch_kernel<EE><<<dim3(g.K, B), fft_threads(g.N, EE), sm, s>>>(g, gwin, tws.first, zbar);
+            const size_t sm = sizeof(float2) * fft_slots(g.N);
+            GBB_DISPATCH_E(E, fft_threads(g.N, E), {
+                BCK((cudaError_t)smem_attr((const void*)colsT_batch_kernel<EE, TT>, sm));
+                colsT_batch_kernel<EE, TT><<<dim3(g.K, B), fft_threads(g.N, EE), sm, s>>>(
+                    g, gwin, ws.stage_tw(g.N, EE), zbar);
             });
             BCK(cudaGetLastError());
         };
         auto rowsT = [&](int E) {
-            const size_t sm = sizeof(float2) * g.M + sizeof(float) * nr;
+            const size_t sm = sizeof(float2) * fft_slots(g.M) + sizeof(float) * nr;
             if (sm > 220 * 1024) throw Err{GALARIO_EINVAL, "Error in batch: nxy/nr too large for the row adjoint"};
-            GBB_DISPATCH_E(E, {
-                BCK((cudaError_t)smem_attr((const void*)rowsT_batch_kernel<EE>, sm));
-                rowsT_batch_kernel<EE><<<dim3((g.R + kRowsPerCta - 1) / kRowsPerCta, B), fft_threads(g.M, EE), sm, s>>>(
-                    g, intensity, mc, tws.first, tws.second, zbar, grad_intensity, ginc_d, gcentral);
+            GBB_DISPATCH_E(E, fft_threads(g.M, E), {
+                BCK((cudaError_t)smem_attr((const void*)rowsT_batch_kernel<EE, TT>, sm));
+                rowsT_batch_kernel<EE, TT><<<dim3((g.R + kRowsPerCta - 1) / kRowsPerCta, B), fft_threads(g.M, EE), sm, s>>>(
+                    g, intensity, mc, ws.stage_tw(g.M, EE), tws.second, zbar, grad_intensity, ginc_d, gcentral);
             });
             BCK(cudaGetLastError());
         };

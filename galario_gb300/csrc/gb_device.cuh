@@ -8,6 +8,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "gb_internal.cuh"
 
 namespace gbg {
@@ -77,10 +79,53 @@ template <typename T> struct Dft<T, 8> {
     }
 };
 
+// Shared-memory slot of FFT element i: one padding slot every 16 elements, so
+// the power-of-two strides of the Stockham writes do not hit one bank.
+__host__ __device__ __forceinline__ int sp(int i) { return i + (i >> 4); }
+// shared-memory slots for an FFT of length L
+__host__ __device__ __forceinline__ size_t fft_slots(int L) { return (size_t)L + (size_t)(L >> 4) + 1; }
+
+template <typename T> struct Dft<T, 16> {
+    using CT = C2<T>;
+    // 16 = 4 x 4: n = 4 n1 + n2, k = k1 + 4 k2,
+    // X[k1 + 4 k2] = sum_n2 W16^(n2 k1) W4^(n2 k2) sum_n1 x[4 n1 + n2] W4^(n1 k1)
+    __device__ __forceinline__ static void run(CT* v) {
+        const T c1 = (T)0.92387953251128675613, s1 = (T)0.38268343236508977173;
+        const T h = sqrt_half<T>();
+        CT a[4][4];
+#pragma unroll
+        for (int n2 = 0; n2 < 4; ++n2) {
+            CT t[4] = {v[n2], v[4 + n2], v[8 + n2], v[12 + n2]};
+            Dft<T, 4>::run(t);
+#pragma unroll
+            for (int k1 = 0; k1 < 4; ++k1) a[n2][k1] = t[k1];
+        }
+        // twiddles W16^m = exp(-2 pi i m / 16)
+        a[1][1] = cmul(a[1][1], CT{c1, -s1});
+        a[1][2] = cmul(a[1][2], CT{h, -h});
+        a[1][3] = cmul(a[1][3], CT{s1, -c1});
+        a[2][1] = cmul(a[2][1], CT{h, -h});
+        a[2][2] = cmul_mi(a[2][2]);
+        a[2][3] = cmul(a[2][3], CT{-h, -h});
+        a[3][1] = cmul(a[3][1], CT{s1, -c1});
+        a[3][2] = cmul(a[3][2], CT{-h, -h});
+        a[3][3] = cmul(a[3][3], CT{-c1, s1});
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1) {
+            CT t[4] = {a[0][k1], a[1][k1], a[2][k1], a[3][k1]};
+            Dft<T, 4>::run(t);
+#pragma unroll
+            for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = t[k2];
+        }
+    }
+};
+
 // One Stockham stage of radix R on buf[0, M) (in place, two barriers).
-// Every thread owns E/R butterflies.  tw[m] = exp(-2 pi i m / twN), twN = tw_mul * M.
+// Every thread owns E/R butterflies.  stw holds this stage's twiddles
+// W^(r k) = exp(-2 pi i r k / (Ns R)) at stw[(r - 1) * Ns + k], r in [1, R),
+// k in [0, Ns): consecutive threads read consecutive entries.
 template <typename T, int E, int R>
-__device__ __forceinline__ void stockham_stage(C2<T>* buf, int M, int Ns, const C2<T>* __restrict__ tw, int tw_mul) {
+__device__ __forceinline__ void stockham_stage(C2<T>* buf, int M, int Ns, const C2<T>* __restrict__ stw) {
     using CT = C2<T>;
     constexpr int B = E / R;
     const int nt = blockDim.x, tid = threadIdx.x;
@@ -90,7 +135,7 @@ __device__ __forceinline__ void stockham_stage(C2<T>* buf, int M, int Ns, const 
     for (int b = 0; b < B; ++b) {
         const int j = tid + b * nt;
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[b * R + r] = buf[j + r * stride];
+        for (int r = 0; r < R; ++r) v[b * R + r] = buf[sp(j + r * stride)];
     }
     __syncthreads();
 #pragma unroll
@@ -98,14 +143,13 @@ __device__ __forceinline__ void stockham_stage(C2<T>* buf, int M, int Ns, const 
         const int j = tid + b * nt;
         const int k = j & (Ns - 1);
         if (Ns > 1) {
-            const int step = k * tw_mul * (M / (Ns * R));
 #pragma unroll
-            for (int r = 1; r < R; ++r) v[b * R + r] = cmul(v[b * R + r], __ldg(&tw[r * step]));
+            for (int r = 1; r < R; ++r) v[b * R + r] = cmul(v[b * R + r], __ldg(&stw[(r - 1) * Ns + k]));
         }
         Dft<T, R>::run(&v[b * R]);
         const int d = (j - k) * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) buf[d + r * Ns] = v[b * R + r];
+        for (int r = 0; r < R; ++r) buf[sp(d + r * Ns)] = v[b * R + r];
     }
     __syncthreads();
 }
@@ -114,15 +158,35 @@ template <typename T> struct Dft<T, 1> {
     __device__ __forceinline__ static void run(C2<T>*) {}
 };
 
+// radix of the next stage for E values per thread and `bits` = log2 of the
+// remaining length; the host builds the stage twiddles with the same rule
+__host__ __device__ __forceinline__ int stage_radix(int E, int bits) {
+    if (E >= 16 && bits >= 4) return 16;
+    if (E >= 8 && bits >= 3) return 8;
+    if (E >= 4 && bits >= 2) return 4;
+    return 2;
+}
+
 // Forward complex FFT of length M = E * blockDim.x (power of two) on shared
-// memory, natural order in and out.
+// memory (padded slots, sp()), natural order in and out.  stw: the stage
+// twiddles of (M, E), stage after stage.
 template <typename T, int E>
-__device__ void block_fft(C2<T>* buf, int M, int log2M, const C2<T>* __restrict__ tw, int tw_mul) {
+__device__ void block_fft(C2<T>* buf, int M, int log2M, const C2<T>* __restrict__ stw) {
     int Ns = 1, bits = log2M;
     while (bits > 0) {
+        if constexpr (E >= 16) {
+            if (bits >= 4) {
+                stockham_stage<T, E, 16>(buf, M, Ns, stw);
+                stw += 15 * Ns;
+                Ns <<= 4;
+                bits -= 4;
+                continue;
+            }
+        }
         if constexpr (E >= 8) {
             if (bits >= 3) {
-                stockham_stage<T, E, 8>(buf, M, Ns, tw, tw_mul);
+                stockham_stage<T, E, 8>(buf, M, Ns, stw);
+                stw += 7 * Ns;
                 Ns <<= 3;
                 bits -= 3;
                 continue;
@@ -130,20 +194,50 @@ __device__ void block_fft(C2<T>* buf, int M, int log2M, const C2<T>* __restrict_
         }
         if constexpr (E >= 4) {
             if (bits >= 2) {
-                stockham_stage<T, E, 4>(buf, M, Ns, tw, tw_mul);
+                stockham_stage<T, E, 4>(buf, M, Ns, stw);
+                stw += 3 * Ns;
                 Ns <<= 2;
                 bits -= 2;
                 continue;
             }
         }
         if constexpr (E >= 2) {
-            stockham_stage<T, E, 2>(buf, M, Ns, tw, tw_mul);
+            stockham_stage<T, E, 2>(buf, M, Ns, stw);
+            stw += Ns;
             Ns <<= 1;
             bits -= 1;
         } else {
             bits = 0;  // E == 1 means M == 1: nothing to do
         }
     }
+}
+
+// Stage twiddles of a length-L FFT with E values per thread (host side):
+// for each stage (radix R, span Ns), W^(r k) for r in [1, R), k in [0, Ns),
+// evaluated in long double.
+template <typename T> inline std::vector<C2<T>> stage_twiddles(int L, int E) {
+    std::vector<C2<T>> out;
+    int bits = 0;
+    while ((1 << bits) < L) ++bits;
+    int Ns = 1;
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    while (bits > 0) {
+        const int R = stage_radix(E, bits);
+        int rb = 0;
+        while ((1 << rb) < R) ++rb;
+        for (int r = 1; r < R; ++r)
+            for (int k = 0; k < Ns; ++k) {
+                const long double a = -two_pi * (long double)r * (long double)k / ((long double)Ns * R);
+                C2<T> w;
+                w.x = (T)cosl(a);
+                w.y = (T)sinl(a);
+                out.push_back(w);
+            }
+        Ns *= R;
+        bits -= rb;
+    }
+    if (out.empty()) out.push_back(C2<T>{(T)1, (T)0});
+    return out;
 }
 
 __device__ __forceinline__ int ilog2(int n) { return 31 - __clz(n); }
@@ -172,8 +266,8 @@ template <typename T> __device__ __forceinline__ T tw_cast(double x) { return (T
 template <typename T>
 __device__ __forceinline__ C2<T> real_split(const C2<T>* Z, int M, int k, const C2<T>* __restrict__ tw) {
     using CT = C2<T>;
-    const CT za = Z[k == M ? 0 : k];
-    const CT zb = Z[k == 0 ? 0 : M - k];
+    const CT za = Z[sp(k == M ? 0 : k)];
+    const CT zb = Z[sp(k == 0 ? 0 : M - k)];
     // Ek = (za + conj(zb))/2 ; Ok = (za - conj(zb))/(2i)
     const T h = (T)0.5;
     const CT e = CT{h * (za.x + zb.x), h * (za.y - zb.y)};
@@ -410,13 +504,18 @@ template <typename T> struct FftCfg {
 };
 template <typename T> FftCfg<T> fft_cfg(int M) {
     FftCfg<T> c;
-    if (M >= 16384) c.E = 16;
+    // FP32: radix-16 stages once there are 32+ threads; FP64 keeps 8 values per
+    // thread (16 double2 per thread costs too many registers)
+    if (M >= 16384 || (sizeof(T) == 4 && M >= 512)) c.E = 16;
     else if (M >= 8) c.E = 8;
     else c.E = M < 1 ? 1 : M;
     c.threads = M / c.E < 1 ? 1 : M / c.E;
-    c.smem = sizeof(C2<T>) * (size_t)(M < 1 ? 1 : M);
+    c.smem = sizeof(C2<T>) * fft_slots(M < 1 ? 1 : M);
     return c;
 }
+
+// values per thread of the shared-memory FFT of length M in precision T
+template <typename T> inline int fft_e(int M) { return fft_cfg<T>(M).E; }
 
 template <typename K> cudaError_t set_smem(K kernel, size_t smem) {
     if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -93,20 +93,22 @@ template <typename T> struct Launch {
     // row pass on an image (rows [0, N)), output zt for columns [0, K) where
     // K = host_K if >= 0, else from state->rmax2 (window_from_extent).
     // row_sign: multiply row i by (-1)^i.
-    static cudaError_t rows_image(const T* image, int N, const CT* tw, CT* zt, int host_K, const DevState* state,
-                                  double duv, bool row_sign, cudaStream_t s);
+    // tw: exp(-2 pi i m / N), m in [0, N); stw: stage twiddles of the length-N/2 row FFT
+    static cudaError_t rows_image(const T* image, int N, const CT* tw, const CT* stw, CT* zt, int host_K,
+                                  const DevState* state, double duv, bool row_sign, cudaStream_t s);
     // row pass fused with the profile sweep: only rows [N/2 - rmax, N/2 + rmax) are nonzero
     static cudaError_t rows_profile(const T* intensity, int nr, double Rmin, double dR, double dxy, double cos_inc,
-                                    int rmax, double central_value, int N, const CT* tw, CT* zt, const DevState* state,
-                                    double duv, cudaStream_t s);
+                                    int rmax, double central_value, int N, const CT* tw, const CT* stw, CT* zt,
+                                    const DevState* state, double duv, cudaStream_t s);
     // column pass: column FFTs of zt (rows outside [band0, band1) are zero) and
     // write rows [r0, r0+W) of columns [0, K) to out[(r - r0)*s_row + k*s_col],
     // times (-1)^(r + k + N/2) if out_sign.  host_K/host_r0/host_W >= 0 override
     // the device-derived window.
     // amp_out (optional, same layout as out) receives |out|, so the visibility
     // pass gathers amplitudes instead of recomputing 4 moduli per point.
-    static cudaError_t cols(const CT* zt, int N, int band0, int band1, const CT* tw, CT* out, T* amp_out,
-                            long long s_row, long long s_col, int host_K, int host_r0, int host_W,
+    // stw: stage twiddles of the length-N column FFT
+    static cudaError_t cols(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
+                            T* amp_out, long long s_row, long long s_col, int host_K, int host_r0, int host_W,
                             const DevState* state, double duv, bool out_sign, cudaStream_t s);
     // fused rotation + interpolation + phase + (vis out) + (chi2 reduction)
     struct VisArgs {

@@ -32,9 +32,10 @@ namespace {
 // ---------------------------------------------------------------------------
 // row pass kernels
 // ---------------------------------------------------------------------------
-template <typename T, int E>
-__global__ void __launch_bounds__(1024) rows_image_kernel(const T* __restrict__ image, int N, const C2<T>* __restrict__ tw,
-                                                          C2<T>* __restrict__ zt, int host_K,
+template <typename T, int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) rows_image_kernel(const T* __restrict__ image, int N, const C2<T>* __restrict__ tw,
+                                                          const C2<T>* __restrict__ stw, C2<T>* __restrict__ zt,
+                                                          int host_K,
                                                           const DevState* __restrict__ st, double duv, int row_sign) {
     using CT = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -42,9 +43,9 @@ __global__ void __launch_bounds__(1024) rows_image_kernel(const T* __restrict__ 
     const int M = N / 2;
     const int i = blockIdx.x;
     const CT* row = reinterpret_cast<const CT*>(image + (size_t)i * N);
-    for (int m = threadIdx.x; m < M; m += blockDim.x) buf[m] = __ldg(&row[m]);
+    for (int m = threadIdx.x; m < M; m += blockDim.x) buf[sp(m)] = __ldg(&row[m]);
     __syncthreads();
-    block_fft<T, E>(buf, M, ilog2(M), tw, 2);
+    block_fft<T, E>(buf, M, ilog2(M), stw);
     const int K = get_window(host_K, 0, 0, st).K;
     const T sgn = (row_sign && (i & 1)) ? (T)-1 : (T)1;
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
@@ -53,10 +54,11 @@ __global__ void __launch_bounds__(1024) rows_image_kernel(const T* __restrict__ 
     }
 }
 
-template <typename T, int E>
-__global__ void __launch_bounds__(1024) rows_profile_kernel(const T* __restrict__ intensity, int nr, T Rmin, T dR,
+template <typename T, int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) rows_profile_kernel(const T* __restrict__ intensity, int nr, T Rmin, T dR,
                                                             T inv_dR, T dxy, T inv_cos_inc, int rmax, T central, int N,
-                                                            const C2<T>* __restrict__ tw, C2<T>* __restrict__ zt,
+                                                            const C2<T>* __restrict__ tw,
+                                                            const C2<T>* __restrict__ stw, C2<T>* __restrict__ zt,
                                                             const DevState* __restrict__ st, double duv) {
     using CT = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -73,10 +75,10 @@ __global__ void __launch_bounds__(1024) rows_profile_kernel(const T* __restrict_
             if (J0 == N / 2) a = central;
             if (J1 == N / 2) b = central;
         }
-        buf[m] = CT{a, b};
+        buf[sp(m)] = CT{a, b};
     }
     __syncthreads();
-    block_fft<T, E>(buf, M, ilog2(M), tw, 2);
+    block_fft<T, E>(buf, M, ilog2(M), stw);
     const int K = st->win_K;
     const T sgn = (I & 1) ? (T)-1 : (T)1;
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
@@ -88,9 +90,9 @@ __global__ void __launch_bounds__(1024) rows_profile_kernel(const T* __restrict_
 // ---------------------------------------------------------------------------
 // column pass
 // ---------------------------------------------------------------------------
-template <typename T, int E>
-__global__ void __launch_bounds__(1024) cols_kernel(const C2<T>* __restrict__ zt, int N, int band0, int band1,
-                                                    const C2<T>* __restrict__ tw, C2<T>* __restrict__ out,
+template <typename T, int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) cols_kernel(const C2<T>* __restrict__ zt, int N, int band0, int band1,
+                                                    const C2<T>* __restrict__ stw, C2<T>* __restrict__ out,
                                                     T* __restrict__ amp_out, long long s_row, long long s_col,
                                                     int host_K, int host_r0,
                                                     int host_W, const DevState* __restrict__ st, double duv,
@@ -103,13 +105,13 @@ __global__ void __launch_bounds__(1024) cols_kernel(const C2<T>* __restrict__ zt
     if (k >= w.K) return;  // uniform for the whole block
     const CT* col = zt + (size_t)k * N;
     for (int i = threadIdx.x; i < N; i += blockDim.x)
-        buf[i] = (i >= band0 && i < band1) ? __ldg(&col[i]) : CT{(T)0, (T)0};
+        buf[sp(i)] = (i >= band0 && i < band1) ? __ldg(&col[i]) : CT{(T)0, (T)0};
     __syncthreads();
-    block_fft<T, E>(buf, N, ilog2(N), tw, 1);
+    block_fft<T, E>(buf, N, ilog2(N), stw);
     const int par = (k + N / 2) & 1;
     for (int q = threadIdx.x; q < w.W; q += blockDim.x) {
         const int r = w.r0 + q;
-        CT x = buf[r];
+        CT x = buf[sp(r)];
         if (out_sign && ((r & 1) ^ par)) x = cneg(x);
         const long long o = (long long)q * s_row + (long long)k * s_col;
         out[o] = x;
@@ -607,28 +609,36 @@ cudaError_t Launch<T>::extent(const T* u, const T* v, int nd, int N, double duv,
     return cudaGetLastError();
 }
 
-#define GBG_DISPATCH_E(E_, ...)                                   \
-    switch (E_) {                                                 \
-        case 1: { constexpr int EE = 1; __VA_ARGS__; } break;     \
-        case 2: { constexpr int EE = 2; __VA_ARGS__; } break;     \
-        case 4: { constexpr int EE = 4; __VA_ARGS__; } break;     \
-        case 8: { constexpr int EE = 8; __VA_ARGS__; } break;     \
-        case 16: { constexpr int EE = 16; __VA_ARGS__; } break;   \
-        default: return cudaErrorInvalidValue;                    \
+// (values per thread EE, block-size bound TT) for an FFT with `threads` threads
+#define GBG_CASE_T(E_V, THR, ...)                                                          \
+    {                                                                                      \
+        constexpr int EE = E_V;                                                            \
+        if ((THR) <= 256) { constexpr int TT = 256; __VA_ARGS__; }                         \
+        else if ((THR) <= 512) { constexpr int TT = 512; __VA_ARGS__; }                    \
+        else { constexpr int TT = 1024; __VA_ARGS__; }                                     \
+    }
+#define GBG_DISPATCH_E(E_, THR, ...)                                              \
+    switch (E_) {                                                                 \
+        case 1: { constexpr int EE = 1; constexpr int TT = 256; __VA_ARGS__; } break; \
+        case 2: { constexpr int EE = 2; constexpr int TT = 256; __VA_ARGS__; } break; \
+        case 4: { constexpr int EE = 4; constexpr int TT = 256; __VA_ARGS__; } break; \
+        case 8: GBG_CASE_T(8, THR, __VA_ARGS__) break;                             \
+        case 16: GBG_CASE_T(16, THR, __VA_ARGS__) break;                           \
+        default: return cudaErrorInvalidValue;                                    \
     }
 
 template <typename T>
-cudaError_t Launch<T>::rows_image(const T* image, int N, const CT* tw, CT* zt, int host_K, const DevState* state,
-                                  double duv, bool row_sign, cudaStream_t s) {
+cudaError_t Launch<T>::rows_image(const T* image, int N, const CT* tw, const CT* stw, CT* zt, int host_K,
+                                  const DevState* state, double duv, bool row_sign, cudaStream_t s) {
     if (is_pow2(N) && N <= max_fft_n_impl<T>() * 2) {
         const int M = N / 2;
         FftCfg<T> c = fft_cfg<T>(M);
         cudaError_t e = cudaSuccess;
-        GBG_DISPATCH_E(c.E, {
-            auto kern = rows_image_kernel<T, EE>;
+        GBG_DISPATCH_E(c.E, c.threads, {
+            auto kern = rows_image_kernel<T, EE, TT>;
             e = set_smem(kern, c.smem);
             if (e == cudaSuccess) {
-                kern<<<N, c.threads, c.smem, s>>>(image, N, tw, zt, host_K, state, duv, row_sign ? 1 : 0);
+                kern<<<N, c.threads, c.smem, s>>>(image, N, tw, stw, zt, host_K, state, duv, row_sign ? 1 : 0);
                 e = cudaGetLastError();
             }
         });
@@ -644,7 +654,7 @@ cudaError_t Launch<T>::rows_image(const T* image, int N, const CT* tw, CT* zt, i
 
 template <typename T>
 cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, double dR, double dxy, double cos_inc,
-                                    int rmax, double central_value, int N, const CT* tw, CT* zt,
+                                    int rmax, double central_value, int N, const CT* tw, const CT* stw, CT* zt,
                                     const DevState* state, double duv, cudaStream_t s) {
     const int nrows = 2 * rmax;
     if (nrows <= 0) return cudaSuccess;
@@ -653,12 +663,12 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
         const int M = N / 2;
         FftCfg<T> c = fft_cfg<T>(M);
         cudaError_t e = cudaSuccess;
-        GBG_DISPATCH_E(c.E, {
-            auto kern = rows_profile_kernel<T, EE>;
+        GBG_DISPATCH_E(c.E, c.threads, {
+            auto kern = rows_profile_kernel<T, EE, TT>;
             e = set_smem(kern, c.smem);
             if (e == cudaSuccess) {
                 kern<<<nrows, c.threads, c.smem, s>>>(intensity, nr, (T)Rmin, (T)dR, (T)(1.0 / dR), (T)dxy,
-                                                      inv_cos, rmax, (T)central_value, N, tw, zt, state, duv);
+                                                      inv_cos, rmax, (T)central_value, N, tw, stw, zt, state, duv);
                 e = cudaGetLastError();
             }
         });
@@ -673,8 +683,8 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
 }
 
 template <typename T>
-cudaError_t Launch<T>::cols(const CT* zt, int N, int band0, int band1, const CT* tw, CT* out, T* amp_out,
-                            long long s_row, long long s_col, int host_K, int host_r0, int host_W,
+cudaError_t Launch<T>::cols(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
+                            T* amp_out, long long s_row, long long s_col, int host_K, int host_r0, int host_W,
                             const DevState* state, double duv, bool out_sign, cudaStream_t s) {
     const int C = N / 2 + 1;
     const int grid = host_K >= 0 ? host_K : C;
@@ -682,11 +692,11 @@ cudaError_t Launch<T>::cols(const CT* zt, int N, int band0, int band1, const CT*
     if (is_pow2(N) && N <= max_fft_n_impl<T>()) {
         FftCfg<T> c = fft_cfg<T>(N);
         cudaError_t e = cudaSuccess;
-        GBG_DISPATCH_E(c.E, {
-            auto kern = cols_kernel<T, EE>;
+        GBG_DISPATCH_E(c.E, c.threads, {
+            auto kern = cols_kernel<T, EE, TT>;
             e = set_smem(kern, c.smem);
             if (e == cudaSuccess) {
-                kern<<<grid, c.threads, c.smem, s>>>(zt, N, band0, band1, tw, out, amp_out, s_row, s_col, host_K,
+                kern<<<grid, c.threads, c.smem, s>>>(zt, N, band0, band1, stw, out, amp_out, s_row, s_col, host_K,
                                                      host_r0, host_W, state, duv, out_sign ? 1 : 0);
                 e = cudaGetLastError();
             }
