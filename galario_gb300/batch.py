@@ -27,12 +27,13 @@ _I = C.c_int
 def _bind():
     L = _lib.lib()
     if not getattr(L, "_gb_batch_bound", False):
-        L.galario_dataset_create_f.argtypes = [_I, _P, _P, _P, _P, _P, _I, C.POINTER(_P)]
+        L.galario_dataset_create_f.argtypes = [_I, _P, _P, _P, _P, _P, _I, _P, _I, C.POINTER(_P)]
         L.galario_dataset_free.argtypes = [_P]
         L.galario_dataset_nvis.argtypes = [_P, C.POINTER(_I)]
-        L.galario_chi2_profile_batch_f.argtypes = [_P, _I, _I, _P, _F, _F, _F, _I, _P, _P, _P, _P, _P]
+        L.galario_dataset_nsets.argtypes = [_P, C.POINTER(_I)]
+        L.galario_chi2_profile_batch_f.argtypes = [_P, _I, _I, _P, _F, _F, _F, _I, _P, _P, _P, _P, _P, _P]
         for n in ("galario_dataset_create_f", "galario_dataset_free", "galario_dataset_nvis",
-                  "galario_chi2_profile_batch_f"):
+                  "galario_dataset_nsets", "galario_chi2_profile_batch_f"):
             getattr(L, n).restype = _I
         L._gb_batch_bound = True
     return L
@@ -42,26 +43,46 @@ class Dataset:
     """Observed visibilities resident on the current GPU (float32 copies).
 
     u, v [wavelengths], re, im [Jy], w [1/Jy^2]: numpy arrays or torch tensors
-    (CPU or CUDA).  The maximum |uv| is computed once here, so the spectrum
-    window of every later call is known without a device round trip.
+    (CPU or CUDA), or lists of them, one entry per visibility set (for example
+    one per spectral window or per observation; the sets may differ in
+    length).  chi2 is additive over the sets: ``chi2_profile_batch`` returns
+    the total, or with ``per_set=True`` one chi2 per set.  The maximum |uv|
+    over all sets is computed once here, so the spectrum window of every later
+    call is known without a device round trip.
     """
 
     def __init__(self, u, v, re, im, w):
         import torch
-        arrs = []
-        for a in (u, v, re, im, w):
-            t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a))
-            t = t.to(device="cuda", dtype=torch.float32).contiguous()
-            arrs.append(t)
+        cols = [u, v, re, im, w]
+        if isinstance(u, (list, tuple)):
+            nsets = len(u)
+            if nsets == 0 or any(not isinstance(c, (list, tuple)) or len(c) != nsets for c in cols):
+                raise ValueError("u, v, re, im, w must be lists of the same length (one entry per set)")
+        else:
+            nsets = 1
+            cols = [[c] for c in cols]
+
+        def flat(parts):
+            ts = [p if isinstance(p, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(p)) for p in parts]
+            ts = [t.reshape(-1).to(device="cuda", dtype=torch.float32) for t in ts]
+            return ts
+        per = [flat(c) for c in cols]
+        lengths = [t.numel() for t in per[0]]
+        for c in per:
+            if [t.numel() for t in c] != lengths:
+                raise AssertionError("Wrong array length: u, v, re, im, w must have the same length")
+        arrs = [torch.cat(c).contiguous() for c in per]
         n = arrs[0].numel()
-        if any(t.numel() != n for t in arrs):
-            raise AssertionError("Wrong array length: u, v, re, im, w must have the same length")
+        offsets = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int32)
         L = _bind()
         h = _P()
         torch.cuda.synchronize()
-        _lib.check(L.galario_dataset_create_f(n, *(t.data_ptr() for t in arrs), 1, C.byref(h)))
+        _lib.check(L.galario_dataset_create_f(n, *(t.data_ptr() for t in arrs), nsets,
+                                              offsets.ctypes.data_as(_P), 1, C.byref(h)))
         self._h = h
         self.nd = n
+        self.nsets = nsets
+        self.nvis_per_set = lengths
 
     @property
     def handle(self):
@@ -79,13 +100,14 @@ class Dataset:
             pass
 
 
-def chi2_profile_batch(dataset: Dataset, intensity, params, Rmin, dR, dxy, nxy, grad=False):
+def chi2_profile_batch(dataset: Dataset, intensity, params, Rmin, dR, dxy, nxy, grad=False, per_set=False):
     """chi2 of B profile models against ``dataset``.
 
     intensity: (B, nr) float32 CUDA tensor [Jy/sr] on R = Rmin + i dR;
     params: (B, 4) float32 CUDA tensor of (inc, PA, dRA, dDec) [rad].
-    Returns chi2 (B,) float64, and with grad=True also dchi2/dintensity (B, nr)
-    and dchi2/dparams (B, 4), both float32.
+    Returns chi2 float64, (B,) summed over the dataset's sets or (B, nsets)
+    with per_set=True; with grad=True also dchi2/dintensity (B, nr) and
+    dchi2/dparams (B, 4) of the total chi2, both float32.
     """
     import torch
     intensity = intensity.to(dtype=torch.float32).contiguous()
@@ -99,12 +121,15 @@ def chi2_profile_batch(dataset: Dataset, intensity, params, Rmin, dR, dxy, nxy, 
     B, nr = intensity.shape
     dev = intensity.device
     chi2 = torch.empty(B, dtype=torch.float64, device=dev)
+    sets = torch.empty((B, dataset.nsets), dtype=torch.float64, device=dev) if per_set else None
     gI = torch.empty_like(intensity) if grad else None
     gp = torch.empty_like(params) if grad else None
     stream = torch.cuda.current_stream(dev).cuda_stream
     L = _bind()
     _lib.check(L.galario_chi2_profile_batch_f(dataset.handle, B, nr, intensity.data_ptr(), _F(Rmin), _F(dR),
                                               _F(dxy), int(nxy), params.data_ptr(), chi2.data_ptr(),
+                                              sets.data_ptr() if per_set else None,
                                               gI.data_ptr() if grad else None, gp.data_ptr() if grad else None,
                                               _P(stream)))
-    return (chi2, gI, gp) if grad else chi2
+    out = sets if per_set else chi2
+    return (out, gI, gp) if grad else out

@@ -28,12 +28,17 @@
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <atomic>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/galario_gb300.h"
@@ -46,6 +51,7 @@ void set_error_message(const std::string& msg);  // gb_api.cu
 namespace {
 
 constexpr int kVisThreads = 256;
+constexpr int kVisWarps = kVisThreads / 32;
 constexpr int kRowsPerCta = 4;  // image rows per CTA in the row adjoint
 constexpr int kRec = 16;        // floats per forward cell record (QUAD_REC)
 constexpr int kGRec = 12;       // floats per gradient cell record
@@ -328,10 +334,10 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
     const int b0 = blockIdx.y * Bg;
     const int nb = min(Bg, B - b0);
     ModelConst* smc = reinterpret_cast<ModelConst*>(smem_raw);
-    double* sacc = reinterpret_cast<double*>(smc + Bg);  // [Bg][kAcc]
-    __shared__ float red[kAcc][kVisThreads / 32];
+    // per-warp sums [Bg][kAcc][warps]: every slot is written once, no zeroing
+    // and no barrier between models
+    float* wacc = reinterpret_cast<float*>(smc + Bg);
     for (int i = threadIdx.x; i < nb; i += blockDim.x) smc[i] = mc[b0 + i];
-    for (int i = threadIdx.x; i < Bg * kAcc; i += blockDim.x) sacc[i] = 0.0;
     // this thread's points
     float pu[PTS], pv[PTS], pre[PTS], pim[PTS], pw[PTS];
     const long long base = (long long)blockIdx.x * kVisThreads * PTS + threadIdx.x;
@@ -417,8 +423,11 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
                 const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || key != prev);
                 if (heads != 0xffffffffu) {
                     const int seg = __popc(heads & ((2u << lane) - 1u));
-#pragma unroll
-                    for (int d = 1; d < 32; d <<= 1) {
+                    // only as many halving steps as the longest run needs
+                    const unsigned later = heads & ~((2u << lane) - 1u);
+                    const int run = ((heads >> lane) & 1u) ? (later ? __ffs(later) - 1 : 32) - lane : 0;
+                    const int maxrun = __reduce_max_sync(0xffffffffu, run);
+                    for (int d = 1; d < maxrun; d <<= 1) {
                         const int seg_d = __shfl_down_sync(0xffffffffu, seg, d);
 #pragma unroll
                         for (int cc = 0; cc < 12; ++cc) {
@@ -435,38 +444,51 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
                 }
             }
         }
-        // block reduction of this model's accumulators
+        // warp sums of this model's accumulators
 #pragma unroll
         for (int a = 0; a < (GRAD ? kAcc : 1); ++a) {
             float x = acc[a];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            if (lane == 0) red[a][wid] = x;
+            if (lane == 0) wacc[(bl * kAcc + a) * kVisWarps + wid] = x;
         }
-        __syncthreads();
-        if (threadIdx.x < (GRAD ? kAcc : 1)) {
-            double s = 0.0;
-            for (int q = 0; q < kVisThreads / 32; ++q) s += (double)red[threadIdx.x][q];
-            sacc[bl * kAcc + threadIdx.x] = s;
-        }
-        __syncthreads();
     }
     if (err) atomicOr(&st->err, err);
+    __syncthreads();
     double* dst = partials + ((size_t)blockIdx.x * B + b0) * kAcc;
-    for (int i = threadIdx.x; i < nb * kAcc; i += blockDim.x) dst[i] = sacc[i];
+    for (int i = threadIdx.x; i < nb * kAcc; i += blockDim.x) {
+        double s = 0.0;
+        if (GRAD || (i % kAcc) == 0) {
+            for (int q = 0; q < kVisWarps; ++q) s += (double)wacc[i * kVisWarps + q];
+        }
+        dst[i] = s;
+    }
 }
 
-// partials [blocks][B][kAcc] -> out[b][a] (fixed summation order)
-__global__ void batch_finalize_kernel(int B, int nblocks, const double* __restrict__ partials,
-                                      double* __restrict__ chi2, double* __restrict__ gsum) {
+// partials [blocks][B][kAcc] -> chi2 per set and in total, gradient sums
+// (fixed summation order).  Set k owns the blocks [pad[k], pad[k+1]) / bpts.
+__global__ void batch_finalize_kernel(int B, int nsets, const long long* __restrict__ pad, int bpts,
+                                      const double* __restrict__ partials, double* __restrict__ chi2,
+                                      double* __restrict__ chi2_sets, double* __restrict__ gsum) {
     __shared__ double sh[32];
     const int b = blockIdx.x, a = blockIdx.y;
-    double s = 0.0;
-    for (int q = threadIdx.x; q < nblocks; q += blockDim.x) s += partials[((size_t)q * B + b) * kAcc + a];
-    s = block_sum(s, sh);
-    if (threadIdx.x == 0) {
-        if (a == 0) chi2[b] = s;
-        else gsum[b * kAcc + a] = s;
+    if (a == 0) {
+        double tot = 0.0;
+        for (int k = 0; k < nsets; ++k) {
+            const long long q0 = pad[k] / bpts, q1 = pad[k + 1] / bpts;
+            double s = 0.0;
+            for (long long q = q0 + threadIdx.x; q < q1; q += blockDim.x) s += partials[((size_t)q * B + b) * kAcc];
+            s = block_sum(s, sh);
+            if (threadIdx.x == 0 && chi2_sets) chi2_sets[(size_t)b * nsets + k] = s;
+            tot += s;
+        }
+        if (threadIdx.x == 0) chi2[b] = tot;
+    } else {
+        const long long nblocks = pad[nsets] / bpts;
+        double s = 0.0;
+        for (long long q = threadIdx.x; q < nblocks; q += blockDim.x) s += partials[((size_t)q * B + b) * kAcc + a];
+        s = block_sum(s, sh);
+        if (threadIdx.x == 0) gsum[b * kAcc + a] = s;
     }
 }
 
@@ -693,6 +715,10 @@ Shape default_shape(const Geo& g) {
     sh.pts = 4;
     return sh;
 }
+bool graphs_enabled() {
+    const char* v = std::getenv("GALARIO_GRAPHS");
+    return !(v && v[0] == '0');
+}
 bool autotune_enabled() {
     const char* v = std::getenv("GALARIO_AUTOTUNE");
     return !(v && v[0] == '0');
@@ -728,12 +754,24 @@ struct Tuner {
     }
 };
 
+struct Err {
+    int status;
+    std::string msg;
+};
+
+// bumped whenever a workspace buffer moves: captured graphs older than it are stale
+std::atomic<unsigned long long> g_buf_gen{1};
+// set while a batched call is being captured into a CUDA graph
+thread_local bool t_capturing = false;
+
 struct Buf {
     void* p = nullptr;
     size_t cap = 0;
     template <typename T> T* get(size_t n) {
         size_t bytes = sizeof(T) * (n ? n : 1);
         if (bytes > cap) {
+            if (t_capturing) throw Err{GALARIO_ERUNTIME, "Error in batch: workspace grew during graph capture"};
+            g_buf_gen.fetch_add(1);
             if (p) cudaFree(p);
             p = nullptr;
             cap = 0;
@@ -745,9 +783,37 @@ struct Buf {
     }
 };
 
+// One captured batched call: the launch sequence of a (geometry, dataset,
+// batch size, outputs) combination, reading its inputs from and writing its
+// outputs to the workspace's staging buffers.
+struct GraphKey {
+    TuneKey tk;
+    unsigned long long dataset;  // Dataset::serial
+    float Rmin, dR, dxy;
+    int per_set;
+    bool operator<(const GraphKey& o) const {
+        return std::tie(tk, dataset, Rmin, dR, dxy, per_set) <
+               std::tie(o.tk, o.dataset, o.Rmin, o.dR, o.dxy, o.per_set);
+    }
+};
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long gen = 0;
+    int calls = 0;
+};
+constexpr size_t kMaxGraphs = 32;
+
 struct BatchWs {
     std::mutex mu;
     Buf mc, coef, zt, win, amp, quads, partials, gsum, cgrad, gwin, zbar, ginc, gcentral, gI_tmp, state;
+    Buf in_I, in_p, out_chi2, out_sets, out_gI, out_gp;  // staging of graph launches
+    std::map<GraphKey, GraphEntry> graphs;
+    cudaStream_t cap = nullptr;  // capture stream (captures cannot use the legacy default stream)
+    void drop_graphs() {
+        for (auto& kv : graphs)
+            if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        graphs.clear();
+    }
     std::map<TuneKey, Shape> shapes;
     std::map<std::pair<int, int>, float2*> stw;  // (L, E) -> stage twiddles
     const float2* stage_tw(int L, int E) {
@@ -797,23 +863,30 @@ BatchWs& batch_ws() {
     return *w;
 }
 
+// Visibility sets stored one after the other, each padded with zero-weight
+// entries to a multiple of kSetAlign so that no block of the vis pass straddles
+// two sets; within a set the visibilities are in Morton order.
+constexpr int kSetAlign = kVisThreads * 4;
+std::atomic<unsigned long long> g_dataset_serial{1};
 struct Dataset {
+    unsigned long long serial = g_dataset_serial.fetch_add(1);
     int device = 0;
-    int nd = 0;
+    int nd = 0;       // visibilities given
+    int nd_pad = 0;   // stored entries, padding included
+    int nsets = 1;
+    std::vector<long long> set_pad;  // nsets + 1 offsets into the padded arrays
+    std::vector<int> set_nd;         // visibilities of each set
+    long long* set_pad_d = nullptr;
     float *u = nullptr, *v = nullptr, *re = nullptr, *im = nullptr, *w = nullptr;
     double rmax2 = 0.0;
 };
 
 int smem_attr(const void* kern, size_t smem) {
+    if (t_capturing) return 0;  // set by the eager run that precedes every capture
     if (smem > 48 * 1024)
         return (int)cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     return 0;
 }
-
-struct Err {
-    int status;
-    std::string msg;
-};
 
 #define BCK(x)                                                                                           \
     do {                                                                                                 \
@@ -843,8 +916,10 @@ template <class F> int bguard(F&& f) {
 __global__ void extent_f32_kernel(const float* __restrict__ u, const float* __restrict__ v, int nd,
                                   double* __restrict__ out) {
     float m = 0.f;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += gridDim.x * blockDim.x)
-        m = fmaxf(m, u[i] * u[i] + v[i] * v[i]);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += gridDim.x * blockDim.x) {
+        const float r = u[i] * u[i] + v[i] * v[i];
+        m = (r == r) ? fmaxf(m, r) : __int_as_float(0x7f800000);  // NaN -> +inf: flagged as non-finite
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0 && m > 0.f)
@@ -871,19 +946,41 @@ __global__ void morton_kernel(const float* __restrict__ u, const float* __restri
         idx[i] = i;
     }
 }
-__global__ void gather5_kernel(const int* __restrict__ idx, int nd, const float* __restrict__ a0,
-                               const float* __restrict__ a1, const float* __restrict__ a2,
-                               const float* __restrict__ a3, const float* __restrict__ a4, float* __restrict__ b0,
-                               float* __restrict__ b1, float* __restrict__ b2, float* __restrict__ b3,
-                               float* __restrict__ b4) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += gridDim.x * blockDim.x) {
-        const int j = idx[i];
-        b0[i] = a0[j];
-        b1[i] = a1[j];
-        b2[i] = a2[j];
-        b3[i] = a3[j];
-        b4[i] = a4[j];
+// padded entry p of set k <- raw entry idx[raw[k] + (p - pad[k])], or a
+// zero-weight padding entry past the set's own visibilities
+__global__ void gather_sets_kernel(int nsets, const long long* __restrict__ pad, const long long* __restrict__ raw,
+                                   const int* __restrict__ idx, long long nd_pad, const float* __restrict__ a0,
+                                   const float* __restrict__ a1, const float* __restrict__ a2,
+                                   const float* __restrict__ a3, const float* __restrict__ a4,
+                                   float* __restrict__ b0, float* __restrict__ b1, float* __restrict__ b2,
+                                   float* __restrict__ b3, float* __restrict__ b4) {
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < nd_pad;
+         p += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nsets;  // largest k with pad[k] <= p
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (pad[mid] <= p) lo = mid;
+            else hi = mid;
+        }
+        const long long jj = p - pad[lo];
+        if (jj < raw[lo + 1] - raw[lo]) {
+            const int j = idx[raw[lo] + jj];
+            b0[p] = a0[j];
+            b1[p] = a1[j];
+            b2[p] = a2[j];
+            b3[p] = a3[j];
+            b4[p] = a4[j];
+        } else {
+            b0[p] = 0.f;
+            b1[p] = 0.f;
+            b2[p] = 0.f;
+            b3[p] = 0.f;
+            b4[p] = 0.f;
+        }
     }
+}
+__global__ void iota_kernel(int* __restrict__ idx, int n) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) idx[i] = i;
 }
 
 // (values per thread EE, block-size bound TT) for an FFT with `threads` threads
@@ -909,69 +1006,106 @@ using namespace gbg;
 #define API extern "C" __attribute__((visibility("default")))
 
 API int galario_dataset_create_f(int nd, const float* u, const float* v, const float* re, const float* im,
-                                 const float* w, int on_device, void** handle) {
+                                 const float* w, int nsets, const int* set_offsets, int on_device, void** handle) {
     return bguard([&] {
         if (nd <= 0) throw Err{GALARIO_EINVAL, "Error in dataset: nd must be positive"};
         if (!handle) throw Err{GALARIO_EINVAL, "Error in dataset: handle is NULL"};
-        Dataset* d = new Dataset();
+        if (nsets < 1) throw Err{GALARIO_EINVAL, "Error in dataset: nsets must be positive"};
+        if (!set_offsets && nsets != 1) throw Err{GALARIO_EINVAL, "Error in dataset: set_offsets is NULL"};
+        std::vector<long long> raw((size_t)nsets + 1);
+        for (int k = 0; k <= nsets; ++k) raw[k] = set_offsets ? set_offsets[k] : (k ? nd : 0);
+        if (raw[0] != 0 || raw[nsets] != nd)
+            throw Err{GALARIO_EINVAL, "Error in dataset: set_offsets must start at 0 and end at nd"};
+        std::unique_ptr<Dataset> d(new Dataset());
+        d->nsets = nsets;
+        d->set_pad.assign((size_t)nsets + 1, 0);
+        d->set_nd.assign((size_t)nsets, 0);
+        for (int k = 0; k < nsets; ++k) {
+            const long long n = raw[k + 1] - raw[k];
+            if (n < 0) throw Err{GALARIO_EINVAL, "Error in dataset: set_offsets must not decrease"};
+            d->set_nd[k] = (int)n;
+            d->set_pad[k + 1] = d->set_pad[k] + (n + kSetAlign - 1) / kSetAlign * kSetAlign;
+        }
+        if (d->set_pad[nsets] > (long long)INT_MAX - kSetAlign)
+            throw Err{GALARIO_EINVAL, "Error in dataset: too many visibilities"};
+        const long long nd_pad = d->set_pad[nsets];
         BCK(cudaGetDevice(&d->device));
         d->nd = nd;
-        float** dst[5] = {&d->u, &d->v, &d->re, &d->im, &d->w};
-        const float* src[5] = {u, v, re, im, w};
+        d->nd_pad = (int)nd_pad;
         const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+        const float* src[5] = {u, v, re, im, w};
+        float* raw_d[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+        float** dst[5] = {&d->u, &d->v, &d->re, &d->im, &d->w};
+        unsigned *k0 = nullptr, *k1 = nullptr;
+        int *i0 = nullptr, *i1 = nullptr;
+        long long* raw_off_d = nullptr;
+        double* r2 = nullptr;
+        void* cub_tmp = nullptr;
+        auto cleanup = [&] {
+            for (float* t : raw_d) cudaFree(t);
+            cudaFree(k0); cudaFree(k1); cudaFree(i0); cudaFree(i1);
+            cudaFree(raw_off_d); cudaFree(r2); cudaFree(cub_tmp);
+        };
         try {
             for (int i = 0; i < 5; ++i) {
-                BCK(cudaMalloc(dst[i], sizeof(float) * (size_t)nd));
-                BCK(cudaMemcpy(*dst[i], src[i], sizeof(float) * (size_t)nd, kind));
+                BCK(cudaMalloc(&raw_d[i], sizeof(float) * (size_t)nd));
+                BCK(cudaMemcpy(raw_d[i], src[i], sizeof(float) * (size_t)nd, kind));
             }
-            double* r2 = nullptr;
             BCK(cudaMalloc(&r2, sizeof(double)));
             BCK(cudaMemset(r2, 0, sizeof(double)));
-            extent_f32_kernel<<<num_sms() * 4, 256>>>(d->u, d->v, nd, r2);
+            extent_f32_kernel<<<num_sms() * 4, 256>>>(raw_d[0], raw_d[1], nd, r2);
             BCK(cudaGetLastError());
             BCK(cudaMemcpy(&d->rmax2, r2, sizeof(double), cudaMemcpyDeviceToHost));
-            cudaFree(r2);
-            // spatial order (chi2 is a sum: the order changes only the rounding)
+            if (!std::isfinite(d->rmax2)) throw Err{GALARIO_EINVAL, "Error in dataset: u and v must be finite"};
+            BCK(cudaMalloc(&i0, sizeof(int) * (size_t)nd));
+            BCK(cudaMalloc(&i1, sizeof(int) * (size_t)nd));
+            const int* order = i0;
             if (d->rmax2 > 0.0 && std::isfinite(d->rmax2)) {
-                unsigned *k0 = nullptr, *k1 = nullptr;
-                int *i0 = nullptr, *i1 = nullptr;
-                float* tmp[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-                void* cub_tmp = nullptr;
+                // spatial order within each set (chi2 is a sum: the order changes only the rounding)
+                BCK(cudaMalloc(&k0, sizeof(unsigned) * (size_t)nd));
+                BCK(cudaMalloc(&k1, sizeof(unsigned) * (size_t)nd));
+                const float inv_span = (float)(0.5 / (std::sqrt(d->rmax2) * 1.0000001));
+                morton_kernel<<<num_sms() * 4, 256>>>(raw_d[0], raw_d[1], nd, inv_span, k0, i0);
+                BCK(cudaGetLastError());
                 size_t cub_bytes = 0;
-                auto cleanup = [&] {
-                    cudaFree(k0); cudaFree(k1); cudaFree(i0); cudaFree(i1); cudaFree(cub_tmp);
-                    for (float* t : tmp) cudaFree(t);
-                };
-                try {
-                    BCK(cudaMalloc(&k0, sizeof(unsigned) * nd));
-                    BCK(cudaMalloc(&k1, sizeof(unsigned) * nd));
-                    BCK(cudaMalloc(&i0, sizeof(int) * nd));
-                    BCK(cudaMalloc(&i1, sizeof(int) * nd));
-                    const float inv_span = (float)(0.5 / (std::sqrt(d->rmax2) * 1.0000001));
-                    morton_kernel<<<num_sms() * 4, 256>>>(d->u, d->v, nd, inv_span, k0, i0);
-                    BCK(cudaGetLastError());
-                    BCK(cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, k0, k1, i0, i1, nd, 0, 30));
-                    BCK(cudaMalloc(&cub_tmp, cub_bytes));
-                    BCK(cub::DeviceRadixSort::SortPairs(cub_tmp, cub_bytes, k0, k1, i0, i1, nd, 0, 30));
-                    for (int i = 0; i < 5; ++i) BCK(cudaMalloc(&tmp[i], sizeof(float) * nd));
-                    gather5_kernel<<<num_sms() * 4, 256>>>(i1, nd, d->u, d->v, d->re, d->im, d->w, tmp[0], tmp[1],
-                                                          tmp[2], tmp[3], tmp[4]);
-                    BCK(cudaGetLastError());
-                    BCK(cudaDeviceSynchronize());
-                    for (int i = 0; i < 5; ++i) std::swap(*dst[i], tmp[i]);
-                } catch (...) {
-                    cleanup();
-                    throw;
+                for (int k = 0; k < nsets; ++k) {
+                    size_t b = 0;
+                    if (d->set_nd[k] == 0) continue;
+                    BCK(cub::DeviceRadixSort::SortPairs(nullptr, b, k0, k1, i0, i1, d->set_nd[k], 0, 30));
+                    cub_bytes = std::max(cub_bytes, b);
                 }
-                cleanup();
+                BCK(cudaMalloc(&cub_tmp, cub_bytes ? cub_bytes : 16));
+                for (int k = 0; k < nsets; ++k) {
+                    if (d->set_nd[k] == 0) continue;
+                    size_t b = cub_bytes;
+                    BCK(cub::DeviceRadixSort::SortPairs(cub_tmp, b, k0 + raw[k], k1 + raw[k], i0 + raw[k],
+                                                        i1 + raw[k], d->set_nd[k], 0, 30));
+                }
+                order = i1;
+            } else {
+                iota_kernel<<<num_sms() * 4, 256>>>(i0, nd);
+                BCK(cudaGetLastError());
             }
+            BCK(cudaMalloc(&raw_off_d, sizeof(long long) * raw.size()));
+            BCK(cudaMemcpy(raw_off_d, raw.data(), sizeof(long long) * raw.size(), cudaMemcpyHostToDevice));
+            BCK(cudaMalloc(&d->set_pad_d, sizeof(long long) * d->set_pad.size()));
+            BCK(cudaMemcpy(d->set_pad_d, d->set_pad.data(), sizeof(long long) * d->set_pad.size(),
+                           cudaMemcpyHostToDevice));
+            for (int i = 0; i < 5; ++i) BCK(cudaMalloc(dst[i], sizeof(float) * (size_t)nd_pad));
+            gather_sets_kernel<<<num_sms() * 4, 256>>>(nsets, d->set_pad_d, raw_off_d, order, nd_pad, raw_d[0],
+                                                      raw_d[1], raw_d[2], raw_d[3], raw_d[4], d->u, d->v, d->re,
+                                                      d->im, d->w);
+            BCK(cudaGetLastError());
+            BCK(cudaDeviceSynchronize());
         } catch (...) {
+            cleanup();
             for (int i = 0; i < 5; ++i)
                 if (*dst[i]) cudaFree(*dst[i]);
-            delete d;
+            cudaFree(d->set_pad_d);
             throw;
         }
-        *handle = d;
+        cleanup();
+        *handle = d.release();
     });
 }
 
@@ -982,6 +1116,7 @@ API int galario_dataset_free(void* handle) {
         cudaDeviceSynchronize();
         float* p[5] = {d->u, d->v, d->re, d->im, d->w};
         for (float* x : p) cudaFree(x);
+        cudaFree(d->set_pad_d);
         delete d;
     });
 }
@@ -993,9 +1128,16 @@ API int galario_dataset_nvis(void* handle, int* nd) {
     });
 }
 
+API int galario_dataset_nsets(void* handle, int* nsets) {
+    return bguard([&] {
+        if (!handle) throw Err{GALARIO_EINVAL, "Error in dataset: handle is NULL"};
+        *nsets = static_cast<Dataset*>(handle)->nsets;
+    });
+}
+
 API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* intensity, float Rmin, float dR,
-                                     float dxy, int nxy, const float* params, double* chi2, float* grad_intensity,
-                                     float* grad_params, void* stream) {
+                                     float dxy, int nxy, const float* params, double* chi2, double* chi2_sets,
+                                     float* grad_intensity, float* grad_params, void* stream) {
     return bguard([&] {
         Dataset* d = static_cast<Dataset*>(dataset);
         if (!d) throw Err{GALARIO_EINVAL, "Error in batch: dataset is NULL"};
@@ -1014,7 +1156,8 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
         const bool grad = grad_intensity || grad_params;
         if (grad && !(grad_intensity && grad_params))
             throw Err{GALARIO_EINVAL, "Error in batch: pass both gradient outputs or neither"};
-        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        cudaStream_t s = static_cast<cudaStream_t>(stream);  // the launchers below enqueue on `s`
+        const cudaStream_t s_user = s;
         BatchWs& ws = batch_ws();
         std::lock_guard<std::mutex> lk(ws.mu);
 
@@ -1024,6 +1167,13 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
         g.M = nxy / 2;
         g.C = nxy / 2 + 1;
         const double duv = (double)(float)(1.0 / ((double)dxy * nxy));  // as the FP32 module passes it
+        {
+            const double ext = std::sqrt(d->rmax2) / duv;
+            if (!(ext * (1.0 + 2e-6) + 1e-6 + 2.0 < (double)(nxy / 2)))
+                throw Err{GALARIO_EINVAL, "Error in batch: the visibilities reach max|uv|/duv = " +
+                                              std::to_string(ext) + ", beyond the image's uv range (nxy/2 - 2 = " +
+                                              std::to_string(nxy / 2 - 2) + "); increase nxy or reduce dxy"};
+        }
         const Window w = window_from_extent(d->rmax2, duv, nxy);
         g.K = w.K;
         g.r0 = w.r0;
@@ -1074,7 +1224,7 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
         float2* win = ws.win.get<float2>((size_t)B * ncell);
         float* amp = ws.amp.get<float>((size_t)B * ncell);
         float* quads = ws.quads.get<float>((size_t)B * ncell * kRec);
-        const int max_vblocks = (int)((d->nd + (long long)kVisThreads * 2 - 1) / ((long long)kVisThreads * 2));
+        const int max_vblocks = (int)((d->nd_pad + (long long)kVisThreads * 2 - 1) / ((long long)kVisThreads * 2));
         double* partials = ws.partials.get<double>((size_t)max_vblocks * B * kAcc);
         double* gsum = ws.gsum.get<double>((size_t)B * kAcc);
         auto tws = ws.twiddles(nxy);
@@ -1114,13 +1264,13 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
             BCK(cudaGetLastError());
         };
         auto vis = [&](int pts) {
-            const int vb = (int)((d->nd + (long long)kVisThreads * pts - 1) / ((long long)kVisThreads * pts));
-            const size_t vsm = sizeof(ModelConst) * Bg + sizeof(double) * Bg * kAcc;
+            const int vb = (int)((d->nd_pad + (long long)kVisThreads * pts - 1) / ((long long)kVisThreads * pts));
+            const size_t vsm = sizeof(ModelConst) * Bg + sizeof(float) * Bg * kAcc * kVisWarps;
             const dim3 grid(vb, ngroups);
 #define GBB_VIS(G_, P_)                                                                                        \
     do {                                                                                                       \
         BCK((cudaError_t)smem_attr((const void*)vis_batch_kernel<G_, P_>, vsm));                               \
-        vis_batch_kernel<G_, P_><<<grid, kVisThreads, vsm, s>>>(g, B, Bg, d->nd, d->u, d->v, d->re, d->im,    \
+        vis_batch_kernel<G_, P_><<<grid, kVisThreads, vsm, s>>>(g, B, Bg, d->nd_pad, d->u, d->v, d->re, d->im,\
                                                                d->w, mc, quads, cgrad, partials, st);          \
     } while (0)
             if (grad) {
@@ -1162,7 +1312,7 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
 
         // ---- launch shapes: tuned once per geometry ----
         Shape sh = default_shape(g);
-        const TuneKey key{g.N, g.K, g.W, g.R, B, d->nd, grad ? 1 : 0, nr};
+        const TuneKey key{g.N, g.K, g.W, g.R, B, d->nd_pad, grad ? 1 : 0, nr};
         auto it = ws.shapes.find(key);
         if (it != ws.shapes.end()) {
             sh = it->second;
@@ -1189,27 +1339,100 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
             BCK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
         }
 
-        // ---- forward ----
-        model_setup_kernel<<<(B + 31) / 32, 32, 0, s>>>(B, params, intensity, nr, coef_d, ncoef, inv_duv, mc);
-        BCK(cudaGetLastError());
-        rows(sh.e_rows);
-        cols(sh.e_cols);
-        quad_batch_kernel<<<num_sms() * 8, 256, 0, s>>>(g, B, win, amp, quads);
-        BCK(cudaGetLastError());
-        if (grad) zero_grads();
-        const int vblocks = vis(sh.pts);
-        batch_finalize_kernel<<<dim3(B, grad ? kAcc : 1), 256, 0, s>>>(B, vblocks, partials, chi2, gsum);
-        BCK(cudaGetLastError());
-        if (!grad) return;
+        // ---- the launch sequence of one call ----
+        auto run_all = [&] {
+            BCK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
+            model_setup_kernel<<<(B + 31) / 32, 32, 0, s>>>(B, params, intensity, nr, coef_d, ncoef, inv_duv, mc);
+            BCK(cudaGetLastError());
+            rows(sh.e_rows);
+            cols(sh.e_cols);
+            quad_batch_kernel<<<num_sms() * 8, 256, 0, s>>>(g, B, win, amp, quads);
+            BCK(cudaGetLastError());
+            if (grad) zero_grads();
+            vis(sh.pts);
+            batch_finalize_kernel<<<dim3(B, grad ? kAcc : 1), 256, 0, s>>>(
+                B, d->nsets, d->set_pad_d, kVisThreads * sh.pts, partials, chi2, chi2_sets, gsum);
+            BCK(cudaGetLastError());
+            if (!grad) return;
+            // ---- adjoint ----
+            quadT_batch_kernel<<<num_sms() * 8, 256, 0, s>>>(g, B, cgrad, win, amp, gwin);
+            BCK(cudaGetLastError());
+            colsT(sh.e_colsT);
+            rowsT(sh.e_rowsT);
+            central_adjoint_kernel<<<B, 64, 0, s>>>(B, nr, coef_d, ncoef, gcentral, grad_intensity);
+            BCK(cudaGetLastError());
+            write_grad_params_kernel<<<(B + 127) / 128, 128, 0, s>>>(B, gsum, ginc_d, grad_params);
+            BCK(cudaGetLastError());
+        };
 
-        // ---- adjoint ----
-        quadT_batch_kernel<<<num_sms() * 8, 256, 0, s>>>(g, B, cgrad, win, amp, gwin);
-        BCK(cudaGetLastError());
-        colsT(sh.e_colsT);
-        rowsT(sh.e_rowsT);
-        central_adjoint_kernel<<<B, 64, 0, s>>>(B, nr, coef_d, ncoef, gcentral, grad_intensity);
-        BCK(cudaGetLastError());
-        write_grad_params_kernel<<<(B + 127) / 128, 128, 0, s>>>(B, gsum, ginc_d, grad_params);
-        BCK(cudaGetLastError());
+        // First call of a combination: eager (it also sets the kernels'
+        // attributes and creates the tables); from the second on, one
+        // captured CUDA graph per combination, fed through staging buffers.
+        const GraphKey gk{key, d->serial, Rmin, dR, dxy, chi2_sets ? 1 : 0};
+        GraphEntry* ge = nullptr;
+        if (graphs_enabled()) {
+            auto git = ws.graphs.find(gk);
+            if (git == ws.graphs.end()) {
+                if (ws.graphs.size() >= kMaxGraphs) ws.drop_graphs();
+                git = ws.graphs.emplace(gk, GraphEntry{}).first;
+            }
+            ge = &git->second;
+        }
+        if (!ge || ge->calls++ == 0) {
+            run_all();
+            return;
+        }
+        const size_t nI = (size_t)B * nr, nP = (size_t)B * 4, nS = (size_t)B * d->nsets;
+        float* in_I = ws.in_I.get<float>(nI);
+        float* in_p = ws.in_p.get<float>(nP);
+        double* o_chi2 = ws.out_chi2.get<double>((size_t)B);
+        double* o_sets = chi2_sets ? ws.out_sets.get<double>(nS) : nullptr;
+        float* o_gI = grad ? ws.out_gI.get<float>(nI) : nullptr;
+        float* o_gp = grad ? ws.out_gp.get<float>(nP) : nullptr;
+        float* const user_gI = grad_intensity;
+        float* const user_gp = grad_params;
+        double* const user_chi2 = chi2;
+        double* const user_sets = chi2_sets;
+        BCK(cudaMemcpyAsync(in_I, intensity, sizeof(float) * nI, cudaMemcpyDeviceToDevice, s_user));
+        BCK(cudaMemcpyAsync(in_p, params, sizeof(float) * nP, cudaMemcpyDeviceToDevice, s_user));
+        intensity = in_I;
+        params = in_p;
+        chi2 = o_chi2;
+        chi2_sets = o_sets;
+        grad_intensity = o_gI;
+        grad_params = o_gp;
+        if (!ge->exec || ge->gen != g_buf_gen.load()) {
+            if (!ws.cap) BCK(cudaStreamCreateWithFlags(&ws.cap, cudaStreamNonBlocking));
+            cudaGraph_t graph = nullptr;
+            BCK(cudaStreamBeginCapture(ws.cap, cudaStreamCaptureModeThreadLocal));
+            s = ws.cap;
+            t_capturing = true;
+            try {
+                run_all();
+            } catch (...) {
+                t_capturing = false;
+                s = s_user;
+                cudaStreamEndCapture(ws.cap, &graph);
+                if (graph) cudaGraphDestroy(graph);
+                throw;
+            }
+            t_capturing = false;
+            s = s_user;
+            BCK(cudaStreamEndCapture(ws.cap, &graph));
+            if (ge->exec) cudaGraphExecDestroy(ge->exec);
+            ge->exec = nullptr;
+            const cudaError_t ie = cudaGraphInstantiate(&ge->exec, graph, 0);
+            cudaGraphDestroy(graph);
+            BCK(ie);
+            ge->gen = g_buf_gen.load();
+        }
+        BCK(cudaGraphLaunch(ge->exec, s_user));
+        BCK(cudaMemcpyAsync(user_chi2, o_chi2, sizeof(double) * B, cudaMemcpyDeviceToDevice, s_user));
+        if (user_sets)
+            BCK(cudaMemcpyAsync(user_sets, o_sets, sizeof(double) * nS, cudaMemcpyDeviceToDevice, s_user));
+        if (grad) {
+            BCK(cudaMemcpyAsync(user_gI, o_gI, sizeof(float) * nI, cudaMemcpyDeviceToDevice, s_user));
+            BCK(cudaMemcpyAsync(user_gp, o_gp, sizeof(float) * nP, cudaMemcpyDeviceToDevice, s_user));
+        }
     });
 }

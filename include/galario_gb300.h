@@ -196,6 +196,39 @@ int galario_fftshift_f(int nx, int ny, float *data);
 int galario_fftshift_axis0_d(int nrow, int ncol, double *data);
 int galario_fftshift_axis0_f(int nrow, int ncol, float *data);
 
+/* ---- batched FP32 chi2 with gradient (no counterpart in the reference,
+ * which evaluates one model per call and has no derivative).
+ *
+ * A dataset is a device-resident copy of nd visibilities (float32), made of
+ * nsets visibility sets stored one after the other: set k holds the entries
+ * [set_offsets[k], set_offsets[k+1]) of the input arrays (set_offsets has
+ * nsets + 1 entries, starts at 0 and ends at nd; NULL with nsets == 1 means
+ * one set).  on_device != 0: the five input pointers are device pointers.
+ * The copy is reordered (Morton order of (u, v) within each set) and padded
+ * with zero-weight entries; visibilities of weight 0 contribute nothing. */
+int galario_dataset_create_f(int nd, const float *u, const float *v, const float *re, const float *im,
+                             const float *w, int nsets, const int *set_offsets, int on_device, void **handle);
+int galario_dataset_free(void *handle);
+int galario_dataset_nvis(void *handle, int *nd);
+int galario_dataset_nsets(void *handle, int *nsets);
+
+/* chi2 of B radial-profile models against a dataset, on `stream` (a
+ * cudaStream_t; NULL is CUDA's default stream).  Device pointers:
+ *  intensity (B x nr) [Jy/sr] on R = Rmin + i dR, shared radial grid;
+ *  params (B x 4): inc, PA, dRA, dDec [rad] per model;
+ *  chi2 (B, double): total over the dataset's sets;
+ *  chi2_sets (B x nsets, double) or NULL: chi2 of every set;
+ *  grad_intensity (B x nr) and grad_params (B x 4), both or neither (NULL):
+ *  d(total chi2)/d(intensity, params).
+ * Geometry rules as chi2Profile (galario.cpp:101-121 checks), with nxy a
+ * power of two in [16, 16384].  Arithmetic: FP32 FFTs and interpolation;
+ * uv rotation, cell index and phase in double-float; chi2 and the parameter
+ * gradients accumulated in double.  Calls on one device share a workspace
+ * and are serialised by a lock. */
+int galario_chi2_profile_batch_f(void *dataset, int B, int nr, const float *intensity, float Rmin, float dR,
+                                 float dxy, int nxy, const float *params, double *chi2, double *chi2_sets,
+                                 float *grad_intensity, float *grad_params, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

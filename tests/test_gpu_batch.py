@@ -185,3 +185,81 @@ def test_batch_rejects_bad_geometry(case):
         chi2_profile_batch(c["ds"], c["tI"], c["tp"], c["Rmin"], c["dxy"] / 4, c["dxy"], c["nxy"])
     with pytest.raises(ValueError, match="is odd"):
         chi2_profile_batch(c["ds"], c["tI"], c["tp"], c["Rmin"], c["dR"], c["dxy"], 511)
+
+
+def test_batch_visibility_sets(case, oracle_port):
+    """Uneven visibility sets: chi2 per set against the oracle, total and gradient against one set."""
+    from galario_gb300.batch import Dataset, chi2_profile_batch
+    c = case
+    cuts = [0, 7001, 7001 + 25000, len(c["u"])]  # uneven; the last set is short
+    parts = [slice(cuts[k], cuts[k + 1]) for k in range(3)]
+    ds = Dataset(*[[c[k][p] for p in parts] for k in ("u", "v", "re", "im", "w")])
+    assert ds.nsets == 3 and ds.nvis_per_set == [cuts[k + 1] - cuts[k] for k in range(3)]
+    table = chi2_profile_batch(ds, c["tI"], c["tp"], c["Rmin"], c["dR"], c["dxy"], c["nxy"], per_set=True)
+    table = table.cpu().numpy()
+    assert table.shape == (len(c["I"]), 3)
+    orc = oracle_port.get("port", "double")
+    for b in range(len(c["I"])):
+        inc, PA, dRA, dDec = c["params"][b]
+        for k, p in enumerate(parts):
+            ref = orc.chi2Profile(c["I"][b], c["Rmin"], c["dR"], c["nxy"], c["dxy"], c["u"][p], c["v"][p],
+                                  c["re"][p], c["im"][p], c["w"][p], inc=inc, PA=PA, dRA=dRA, dDec=dDec)
+            assert abs(table[b, k] - ref) / ref <= CHI2_TOL, (b, k, table[b, k], ref)
+    tot, gI, gp = chi2_profile_batch(ds, c["tI"], c["tp"], c["Rmin"], c["dR"], c["dxy"], c["nxy"], grad=True)
+    tot1, gI1, gp1 = chi2_profile_batch(c["ds"], c["tI"], c["tp"], c["Rmin"], c["dR"], c["dxy"], c["nxy"], grad=True)
+    tot_fwd = chi2_profile_batch(ds, c["tI"], c["tp"], c["Rmin"], c["dR"], c["dxy"], c["nxy"])
+    np.testing.assert_allclose(tot_fwd.cpu().numpy(), table.sum(axis=1), rtol=1e-14)  # same launches
+    np.testing.assert_allclose(tot.cpu().numpy(), table.sum(axis=1), rtol=CHI2_TOL)
+    np.testing.assert_allclose(tot.cpu().numpy(), tot1.cpu().numpy(), rtol=CHI2_TOL)
+    for b in range(len(c["I"])):
+        assert _rel(gI[b].cpu().numpy(), gI1[b].cpu().numpy()) <= 1e-3
+        assert _rel(gp[b].cpu().numpy(), gp1[b].cpu().numpy()) <= 1e-4
+
+
+def test_batch_rejects_bad_sets():
+    import ctypes as C
+    from galario_gb300 import _lib
+    from galario_gb300.batch import _bind
+    L = _bind()
+    u = np.zeros(8, np.float32)
+    h = C.c_void_p()
+    off = np.array([0, 5, 3, 8], np.int32)  # decreasing
+    p = u.ctypes.data_as(C.c_void_p)
+    st = L.galario_dataset_create_f(8, p, p, p, p, p, 3, off.ctypes.data_as(C.c_void_p), 0, C.byref(h))
+    assert st == _lib.EINVAL
+    off = np.array([0, 5, 7], np.int32)  # does not end at nd
+    st = L.galario_dataset_create_f(8, p, p, p, p, p, 2, off.ctypes.data_as(C.c_void_p), 0, C.byref(h))
+    assert st == _lib.EINVAL
+
+
+def test_batch_graph_replay_matches_eager(case, monkeypatch):
+    """From the second call of a combination on, the call replays a captured CUDA graph."""
+    import torch
+    from galario_gb300.batch import chi2_profile_batch
+    c = case
+    args = (c["Rmin"], c["dR"], c["dxy"], c["nxy"])
+    scales = [1.0, 0.7, 1.3, 0.9]
+    monkeypatch.setenv("GALARIO_GRAPHS", "0")
+    eager = [chi2_profile_batch(c["ds"], c["tI"] * f, c["tp"], *args, grad=True) for f in scales]
+    monkeypatch.setenv("GALARIO_GRAPHS", "1")
+    for f, (e_chi2, e_gI, e_gp) in zip(scales, eager):
+        tI = (c["tI"] * f).clone()  # a fresh input buffer every call
+        chi2, gI, gp = chi2_profile_batch(c["ds"], tI, c["tp"].clone(), *args, grad=True)
+        torch.testing.assert_close(chi2, e_chi2, rtol=0, atol=0)  # fixed-order reduction
+        torch.testing.assert_close(gI, e_gI, rtol=1e-4, atol=1e-6 * float(e_gI.abs().max()))
+        torch.testing.assert_close(gp, e_gp, rtol=1e-4, atol=1e-6 * float(e_gp.abs().max()))
+    # forward-only calls are a separate combination (their own launch shapes)
+    for f in scales[:3]:
+        chi2 = chi2_profile_batch(c["ds"], c["tI"] * f, c["tp"], *args)
+        torch.testing.assert_close(chi2, eager[scales.index(f)][0], rtol=CHI2_TOL, atol=0)
+
+
+def test_batch_rejects_uv_beyond_image(case):
+    from galario_gb300.batch import Dataset, chi2_profile_batch
+    c = case
+    with pytest.raises(ValueError, match="beyond the image's uv range"):
+        chi2_profile_batch(c["ds"], c["tI"], c["tp"], c["Rmin"], c["dR"], c["dxy"] * 4, c["nxy"] // 4)
+    u = c["u"].copy()
+    u[5] = np.nan
+    with pytest.raises(ValueError, match="must be finite"):
+        Dataset(u, c["v"], c["re"], c["im"], c["w"])
