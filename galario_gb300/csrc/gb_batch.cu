@@ -52,8 +52,8 @@ namespace {
 
 constexpr int kVisThreads = 256;
 constexpr int kVisWarps = kVisThreads / 32;
-constexpr int kRowsPerCta = 4;  // image rows per CTA in the row adjoint
-constexpr int kRec = 16;        // floats per forward cell record (QUAD_REC)
+constexpr int kRowsPerCta = 16;  // folded image rows (up to two box rows each) per CTA in the row adjoint
+constexpr int kRec = 12;        // floats per forward cell record: 4 complex corners, 4 moduli (48 B)
 constexpr int kGRec = 12;       // floats per gradient cell record
 
 struct ModelConst {
@@ -107,38 +107,95 @@ __global__ void model_setup_kernel(int B, const float* __restrict__ params, cons
     mc[b] = m;
 }
 
+// The swept image depends on (|x|, |y|) only: pixel (i, j) of the 2 rmax box
+// has the value of the folded pixel (a, c) = (|rmax - i|, |rmax - j|).  A CTA
+// takes F consecutive folded rows a0..a0+F-1; for each it evaluates the
+// rmax + 1 folded pixels once and transforms the box rows rmax - a and
+// rmax + a (one row for a = 0 and for a = rmax, whose mirror rmax + a = 2 rmax
+// lies outside the box).  The 2F transformed rows are two runs of
+// consecutive box rows, staged in shared memory and written column by column
+// as contiguous runs of the row-major-transposed layout zt[b][k][row].
+// e = k * n + j with 0 <= j < n, for e < 2^22, without the integer divider
+// (whose float conversions run on the slow conversion pipe)
+__device__ __forceinline__ void split_index(int e, int n, float inv_n, int* k, int* j) {
+    float fl;
+    int q = floor_i((i2f_small(e) + 0.5f) * inv_n, &fl);
+    int r = e - q * n;
+    if (r < 0) { --q; r += n; }
+    if (r >= n) { ++q; r -= n; }
+    *k = q;
+    *j = r;
+}
+
+__device__ __forceinline__ int fold_rows(const Geo& g, int a0, int F, int* lo0, int* lo1, int* n1) {
+    const int n0 = min(F, g.rmax + 1 - a0);  // folded rows of this CTA
+    *lo0 = g.rmax - (a0 + n0 - 1);           // side 0: box rows rmax - a, a in [a0, a0 + n0)
+    const int s1 = max(a0, 1);               // side 1: box rows rmax + a, 1 <= a <= rmax - 1
+    const int e1 = min(a0 + n0, g.rmax);
+    *lo1 = g.rmax + s1;
+    *n1 = max(0, e1 - s1);
+    return n0;
+}
+
 template <int E, int MAXT>
-__global__ void __launch_bounds__(MAXT) rows_batch_kernel(Geo g, const float* __restrict__ intensity,
+__global__ void __launch_bounds__(MAXT) rows_batch_kernel(Geo g, int F, const float* __restrict__ intensity,
                                                           const ModelConst* __restrict__ mc,
                                                           const float2* __restrict__ tw,
                                                           const float2* __restrict__ stw, float2* __restrict__ zt) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* buf = reinterpret_cast<float2*>(smem_raw);
+    const int S = 2 * F + 1;                                  // staging row stride (odd: no bank conflicts)
+    float2* stg = buf + fft_slots(g.M);                       // [K][S] staged outputs
+    float* val = reinterpret_cast<float*>(stg + (size_t)g.K * S);  // rmax + 1 folded pixels
     const int b = blockIdx.y;
-    const int irow = blockIdx.x;
-    const int I = g.band0 + irow;
+    const int a0 = blockIdx.x * F;
+    int lo0, lo1, n1;
+    const int n0 = fold_rows(g, a0, F, &lo0, &lo1, &n1);
     const int off = g.N / 2 - g.rmax;
     const float* Ib = intensity + (size_t)b * g.nr;
     const ModelConst m = mc[b];
-    for (int mm = threadIdx.x; mm < g.M; mm += blockDim.x) {
-        const int J0 = 2 * mm, J1 = 2 * mm + 1;
-        float a = sweep_pixel<float>(I, J0, Ib, g.nr, g.Rmin, g.dR, g.inv_dR, g.dxy, m.inv_cos_inc, g.rmax, off,
-                                     g.sr_to_px);
-        float c = sweep_pixel<float>(I, J1, Ib, g.nr, g.Rmin, g.dR, g.inv_dR, g.dxy, m.inv_cos_inc, g.rmax, off,
-                                     g.sr_to_px);
-        if (I == g.N / 2) {
-            if (J0 == g.N / 2) a = m.central;
-            if (J1 == g.N / 2) c = m.central;
+    for (int aa = 0; aa < n0; ++aa) {
+        const int a = a0 + aa;
+        __syncthreads();  // val and buf free
+        for (int c = threadIdx.x; c <= g.rmax; c += blockDim.x)
+            val[c] = sweep_pixel<float>(off + g.rmax - a, off + g.rmax - c, Ib, g.nr, g.Rmin, g.dR, g.inv_dR, g.dxy,
+                                        m.inv_cos_inc, g.rmax, off, g.sr_to_px);
+        for (int side = 0; side < 2; ++side) {
+            const int i_box = side ? g.rmax + a : g.rmax - a;
+            if (side && (a == 0 || i_box >= 2 * g.rmax)) break;  // uniform
+            const int I = off + i_box;
+            const int slot = side ? F + (i_box - lo1) : (i_box - lo0);
+            __syncthreads();  // val ready; buf free
+            for (int mm = threadIdx.x; mm < g.M; mm += blockDim.x) {
+                const int j0 = 2 * mm - off, j1 = j0 + 1;
+                float x0 = 0.f, x1 = 0.f;
+                if (j0 >= 0 && j0 < 2 * g.rmax) x0 = val[abs(g.rmax - j0)];
+                if (j1 >= 0 && j1 < 2 * g.rmax) x1 = val[abs(g.rmax - j1)];
+                if (I == g.N / 2) {
+                    if (2 * mm == g.N / 2) x0 = m.central;
+                    if (2 * mm + 1 == g.N / 2) x1 = m.central;
+                }
+                buf[sp(mm)] = make_float2(x0, x1);
+            }
+            __syncthreads();
+            block_fft<float, E>(buf, g.M, ilog2(g.M), stw);
+            const float sgn = (I & 1) ? -1.f : 1.f;
+            for (int k = threadIdx.x; k < g.K; k += blockDim.x) {
+                const float2 x = real_split<float>(buf, g.M, k, tw);
+                stg[k * S + slot] = make_float2(sgn * x.x, sgn * x.y);
+            }
         }
-        buf[sp(mm)] = make_float2(a, c);
     }
     __syncthreads();
-    block_fft<float, E>(buf, g.M, ilog2(g.M), stw);
-    const float sgn = (I & 1) ? -1.f : 1.f;
     float2* out = zt + (size_t)b * g.K * g.R;
-    for (int k = threadIdx.x; k < g.K; k += blockDim.x) {
-        const float2 x = real_split<float>(buf, g.M, k, tw);
-        out[(size_t)k * g.R + irow] = make_float2(sgn * x.x, sgn * x.y);
+    const int nrun = n0 + n1;
+    const float inv_nrun = 1.f / i2f_small(nrun);
+    for (int e = threadIdx.x; e < g.K * nrun; e += blockDim.x) {
+        int k, j;
+        split_index(e, nrun, inv_nrun, &k, &j);
+        const int row = j < n0 ? lo0 + j : lo1 + (j - n0);
+        const int slot = j < n0 ? j : F + (j - n0);
+        out[(size_t)k * g.R + row] = stg[k * S + slot];
     }
 }
 
@@ -570,7 +627,7 @@ __global__ void __launch_bounds__(MAXT) colsT_batch_kernel(Geo g, const float2* 
 // complex FFT (Hermitian weights), then the sweep adjoint into the profile
 // and the inclination.
 template <int E, int MAXT>
-__global__ void __launch_bounds__(MAXT) rowsT_batch_kernel(Geo g, const float* __restrict__ intensity,
+__global__ void __launch_bounds__(MAXT) rowsT_batch_kernel(Geo g, int F, int G, const float* __restrict__ intensity,
                                                            const ModelConst* __restrict__ mc,
                                                            const float2* __restrict__ stw,
                                                            const float2* __restrict__ twc,
@@ -578,8 +635,11 @@ __global__ void __launch_bounds__(MAXT) rowsT_batch_kernel(Geo g, const float* _
                                                            float* __restrict__ gI, double* __restrict__ ginc,
                                                            float* __restrict__ gcentral) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float2* buf = reinterpret_cast<float2*>(smem_raw);           // M complex
-    float* gIs = reinterpret_cast<float*>(buf + fft_slots(g.M));  // nr floats
+    float2* buf = reinterpret_cast<float2*>(smem_raw);               // M complex
+    const int S = 2 * F + 1;                                         // staging row stride (odd: no bank conflicts)
+    float2* stg = buf + fft_slots(g.M);                              // [K][S] staged input rows
+    float* gIs = reinterpret_cast<float*>(stg + (size_t)g.K * S);    // nr floats
+    float* fold = gIs + g.nr;                                        // rmax + 1 floats
     __shared__ double sinc;
     __shared__ int lo_bin, hi_bin;
     const int b = blockIdx.y;
@@ -596,45 +656,80 @@ __global__ void __launch_bounds__(MAXT) rowsT_batch_kernel(Geo g, const float* _
     int my_lo = g.nr, my_hi = -1;  // bins this thread touched
     const int off = g.N / 2 - g.rmax;
     const int M = g.M;
-    for (int rr = 0; rr < kRowsPerCta; ++rr) {
-        const int irow = blockIdx.x * kRowsPerCta + rr;
-        if (irow >= g.R) break;  // uniform
-        const int I = g.band0 + irow;
-        __syncthreads();
-        // Hermitian weights: Y~0 = Re Y0, Y~k = Yk/2 (0<k<M), Y~M = Re YM; zero for k >= K
-        for (int k = threadIdx.x; k < M; k += blockDim.x) {
-            auto yk = [&](int kk) -> float2 {
-                if (kk >= g.K) return make_float2(0.f, 0.f);
-                const float2 y = zb[(size_t)kk * g.R + irow];
-                if (kk == 0 || kk == M) return make_float2(y.x, 0.f);
-                return make_float2(0.5f * y.x, 0.5f * y.y);
+    // G groups of F folded rows per CTA: the profile flush below is paid once
+    // per G * F folded rows, the staging holds one group
+    for (int grp = 0; grp < G; ++grp) {
+    const int a0 = (blockIdx.x * G + grp) * F;
+    if (a0 > g.rmax) break;  // uniform
+    int lo0, lo1, n1;
+    const int n0 = fold_rows(g, a0, F, &lo0, &lo1, &n1);
+    __syncthreads();  // the previous group's rows are consumed
+    {
+        // the group's 2F rows of every column k: two contiguous runs each
+        const int nrun = n0 + n1;
+        const float inv_nrun = 1.f / i2f_small(nrun);
+        for (int e = threadIdx.x; e < g.K * nrun; e += blockDim.x) {
+            int k, j;
+            split_index(e, nrun, inv_nrun, &k, &j);
+            const int row = j < n0 ? lo0 + j : lo1 + (j - n0);
+            const int slot = j < n0 ? j : F + (j - n0);
+            stg[k * S + slot] = zb[(size_t)k * g.R + row];
+        }
+    }
+    for (int ff = 0; ff < n0; ++ff) {
+        const int a = a0 + ff;  // folded row
+        // sum of the pixel adjoints over the (up to) four mirror images
+        // (+-x, +-y) of every folded pixel of this folded row
+        for (int side = 0; side < 2; ++side) {
+            const int i_box = side ? g.rmax + a : g.rmax - a;
+            if (side && (a == 0 || i_box >= 2 * g.rmax)) break;  // uniform
+            const int I = off + i_box;
+            const int slot = side ? F + (i_box - lo1) : (i_box - lo0);
+            __syncthreads();
+            // Hermitian weights: Y~0 = Re Y0, Y~k = Yk/2 (0<k<M), Y~M = Re YM; zero for k >= K
+            for (int k = threadIdx.x; k < M; k += blockDim.x) {
+                auto yk = [&](int kk) -> float2 {
+                    if (kk >= g.K) return make_float2(0.f, 0.f);
+                    const float2 y = stg[kk * S + slot];
+                    if (kk == 0 || kk == M) return make_float2(y.x, 0.f);
+                    return make_float2(0.5f * y.x, 0.5f * y.y);
+                };
+                const float2 ya = yk(k), yc = yk(M - k);
+                // E' = a + conj(c), O' = (a - conj(c)) e^{+2 pi i k/N}, Z = E' + i O'
+                const float2 Ep = make_float2(ya.x + yc.x, ya.y - yc.y);
+                const float2 d = make_float2(ya.x - yc.x, ya.y + yc.y);
+                const float2 w = twc[k];  // e^{+2 pi i k / N}
+                const float2 Op = make_float2(d.x * w.x - d.y * w.y, d.x * w.y + d.y * w.x);
+                // Z = E' + i O', stored conjugated: the inverse FFT is conj(FFT(conj(Z)))
+                buf[sp(k)] = make_float2(Ep.x - Op.y, -(Ep.y + Op.x));
+            }
+            __syncthreads();
+            block_fft<float, E>(buf, M, ilog2(M), stw);
+            const float sgn = (I & 1) ? -1.f : 1.f;
+            // x_bar of box pixel j: conj(z) in buf, x[2m] = Re z, x[2m+1] = Im z = -buf.y
+            auto xbar = [&](int j) {
+                const int J = j + off;
+                const float2 zz = buf[sp(J >> 1)];
+                return sgn * ((J & 1) ? -zz.y : zz.x);
             };
-            const float2 a = yk(k), c = yk(M - k);
-            // E' = a + conj(c), O' = (a - conj(c)) e^{+2 pi i k/N}, Z = E' + i O'
-            const float2 Ep = make_float2(a.x + c.x, a.y - c.y);
-            const float2 d = make_float2(a.x - c.x, a.y + c.y);
-            const float2 w = twc[k];  // e^{+2 pi i k / N}
-            const float2 Op = make_float2(d.x * w.x - d.y * w.y, d.x * w.y + d.y * w.x);
-            // Z = E' + i O', stored conjugated: the inverse FFT is conj(FFT(conj(Z)))
-            buf[sp(k)] = make_float2(Ep.x - Op.y, -(Ep.y + Op.x));
+            for (int c = threadIdx.x; c <= g.rmax; c += blockDim.x) {  // each c stays with one thread
+                float acc = xbar(g.rmax - c);
+                if (c > 0 && c < g.rmax) acc += xbar(g.rmax + c);
+                fold[c] = side ? fold[c] + acc : acc;
+            }
         }
         __syncthreads();
-        block_fft<float, E>(buf, M, ilog2(M), stw);
-        const float sgn = (I & 1) ? -1.f : 1.f;
-        // sweep adjoint over the box pixels of this row
-        const int i_box = I - off;
-        const float y = i2f_small(g.rmax - i_box) * g.dxy;
-        for (int j = threadIdx.x; j < 2 * g.rmax; j += blockDim.x) {
-            const int J = j + off;
-            const float2 zz = buf[sp(J >> 1)];  // conj(z): x[2m] = Re z, x[2m+1] = Im z = -zz.y
-            const float xb = sgn * ((J & 1) ? -zz.y : zz.x);
-            if (I == g.N / 2 && J == g.N / 2) {  // central pixel: its own adjoint
+        // sweep adjoint of the folded row; (a, c) = (0, 0) is the central pixel alone
+        const float y = i2f_small(a) * g.dxy;
+        for (int c = threadIdx.x; c <= g.rmax; c += blockDim.x) {
+            const float xb = fold[c];
+            if (a == 0 && c == 0) {
                 gcentral[b] = xb;
                 continue;
             }
-            const float x = i2f_small(g.rmax - j) * g.dxy;
+            const float x = i2f_small(c) * g.dxy;
             const float xs = x * m.inv_cos_inc;
-            const float r = sqrtf(xs * xs + y * y);
+            const float r = sqrtf(xs * xs + y * y);  // bit-identical to the forward sweep's radius
             const float tR = (r - g.Rmin) * g.inv_dR;
             if (!(tR < (float)(g.nr - 1))) continue;
             int iR = 0;
@@ -644,16 +739,17 @@ __global__ void __launch_bounds__(MAXT) rowsT_batch_kernel(Geo g, const float* _
             }
             const float frac = (r - i2f_small(iR) * g.dR - g.Rmin) * g.inv_dR;
             const float gxs = xb * g.sr_to_px;
+            const float I0 = __ldg(&Ib[iR]), I1 = __ldg(&Ib[iR + 1]);  // issued before the atomics
             atomicAdd(&gIs[iR], gxs * (1.f - frac));
             atomicAdd(&gIs[iR + 1], gxs * frac);
             my_lo = min(my_lo, iR);
             my_hi = max(my_hi, iR + 1);
-            if (r > 0.f) {
-                const float slope = (__ldg(&Ib[iR + 1]) - __ldg(&Ib[iR])) * g.inv_dR;
-                ginc_acc += gxs * slope * (xs * xs * m.tan_inc) / r;  // dr/dinc = xs^2 tan(inc) / r
-            }
+            // dr/dinc = xs^2 tan(inc) / r (r = 0 only at the central pixel, handled above)
+            const float rinv = r > 0.f ? __fdividef(1.f, r) : 0.f;
+            ginc_acc += gxs * ((I1 - I0) * g.inv_dR) * (xs * xs * m.tan_inc) * rinv;
         }
     }
+    }  // groups
     // once per thread (the block may be narrower than a warp for small images)
     atomicMin(&lo_bin, my_lo);
     atomicMax(&hi_bin, my_hi);
@@ -1243,14 +1339,20 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
         if (Bg > B) Bg = B;
         const int ngroups = (B + Bg - 1) / Bg;
 
+        // folded rows per staging group of the row passes: 2F rows x K columns
+        // within 20 KiB; the adjoint runs G groups per CTA to amortise its flush
+        const int Fcap = std::max(1, (int)((20 * 1024) / (sizeof(float2) * 2 * (size_t)g.K) - 1));
+        const int Frows = std::min(4, Fcap);
+        const int GrowsT = std::max(1, kRowsPerCta / Frows);
         // ---- launchers, one per pass, parameterised by the tuned shape ----
         auto fft_threads = [](int L, int E) { return L / E; };
         auto rows = [&](int E) {
-            const size_t sm = sizeof(float2) * fft_slots(g.M);
+            const size_t sm = sizeof(float2) * (fft_slots(g.M) + (size_t)g.K * (2 * Frows + 1)) +
+                              sizeof(float) * (g.rmax + 1);
             GBB_DISPATCH_E(E, fft_threads(g.M, E), {
                 BCK((cudaError_t)smem_attr((const void*)rows_batch_kernel<EE, TT>, sm));
-                rows_batch_kernel<EE, TT><<<dim3(g.R, B), fft_threads(g.M, EE), sm, s>>>(
-                    g, intensity, mc, tws.first, ws.stage_tw(g.M, EE), zt);
+                rows_batch_kernel<EE, TT><<<dim3((g.rmax + Frows) / Frows, B), fft_threads(g.M, EE), sm, s>>>(
+                    g, Frows, intensity, mc, tws.first, ws.stage_tw(g.M, EE), zt);
             });
             BCK(cudaGetLastError());
         };
@@ -1294,12 +1396,13 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
             BCK(cudaGetLastError());
         };
         auto rowsT = [&](int E) {
-            const size_t sm = sizeof(float2) * fft_slots(g.M) + sizeof(float) * nr;
+            const size_t sm = sizeof(float2) * (fft_slots(g.M) + (size_t)g.K * (2 * Frows + 1)) +
+                              sizeof(float) * (nr + g.rmax + 1);
             if (sm > 220 * 1024) throw Err{GALARIO_EINVAL, "Error in batch: nxy/nr too large for the row adjoint"};
             GBB_DISPATCH_E(E, fft_threads(g.M, E), {
                 BCK((cudaError_t)smem_attr((const void*)rowsT_batch_kernel<EE, TT>, sm));
-                rowsT_batch_kernel<EE, TT><<<dim3((g.R + kRowsPerCta - 1) / kRowsPerCta, B), fft_threads(g.M, EE), sm, s>>>(
-                    g, intensity, mc, ws.stage_tw(g.M, EE), tws.second, zbar, grad_intensity, ginc_d, gcentral);
+                rowsT_batch_kernel<EE, TT><<<dim3((g.rmax + Frows * GrowsT) / (Frows * GrowsT), B), fft_threads(g.M, EE), sm, s>>>(
+                    g, Frows, GrowsT, intensity, mc, ws.stage_tw(g.M, EE), tws.second, zbar, grad_intensity, ginc_d, gcentral);
             });
             BCK(cudaGetLastError());
         };
