@@ -1,11 +1,13 @@
-"""Batched FP32 chi2 (and its gradient) of many profile models on the GPU.
+"""Batched FP32 chi2 (and its gradient) of many models on the GPU.
 
 New surface beside the reference's API (the reference evaluates one model per
-call and has no gradient): a device-resident ``Dataset`` and
+call and has no gradient): a device-resident ``Dataset``;
 ``chi2_profile_batch``, which evaluates B radial-profile models (shared radial
 grid, per-model inclination, position angle and offsets) against one dataset
 in one set of launches, optionally with the gradient of every chi2 with
-respect to the profile samples and to (inc, PA, dRA, dDec).
+respect to the profile samples and to (inc, PA, dRA, dDec); and
+``chi2_image_batch``, the same for B free-form images with the gradient with
+respect to every pixel and to (PA, dRA, dDec).
 
 Arrays are torch CUDA tensors (float32); chi2 comes back as float64.  Units
 as in galario: radians for Rmin, dR, dxy, inc, PA, dRA, dDec; wavelengths for
@@ -32,8 +34,9 @@ def _bind():
         L.galario_dataset_nvis.argtypes = [_P, C.POINTER(_I)]
         L.galario_dataset_nsets.argtypes = [_P, C.POINTER(_I)]
         L.galario_chi2_profile_batch_f.argtypes = [_P, _I, _I, _P, _F, _F, _F, _I, _P, _P, _P, _P, _P, _P]
+        L.galario_chi2_image_batch_f.argtypes = [_P, _I, _I, _P, _F, _F, _P, _P, _P, _P, _P, _P]
         for n in ("galario_dataset_create_f", "galario_dataset_free", "galario_dataset_nvis",
-                  "galario_dataset_nsets", "galario_chi2_profile_batch_f"):
+                  "galario_dataset_nsets", "galario_chi2_profile_batch_f", "galario_chi2_image_batch_f"):
             getattr(L, n).restype = _I
         L._gb_batch_bound = True
     return L
@@ -131,5 +134,46 @@ def chi2_profile_batch(dataset: Dataset, intensity, params, Rmin, dR, dxy, nxy, 
                                               sets.data_ptr() if per_set else None,
                                               gI.data_ptr() if grad else None, gp.data_ptr() if grad else None,
                                               _P(stream)))
+    out = sets if per_set else chi2
+    return (out, gI, gp) if grad else out
+
+
+def chi2_image_batch(dataset: Dataset, images, params, dxy, origin="upper", grad=False, per_set=False):
+    """chi2 of B images against ``dataset`` (chi2Image semantics per image).
+
+    images: (B, nxy, nxy) float32 CUDA tensor [Jy/pixel], nxy a power of two;
+    params: (B, 3) float32 CUDA tensor of (PA, dRA, dDec) [rad];
+    origin: 'upper' or 'lower', as chi2Image.  Returns chi2 float64, (B,) or
+    (B, nsets) with per_set=True; with grad=True also dchi2/dimages
+    (B, nxy, nxy) and dchi2/dparams (B, 3), both float32.
+    """
+    import torch
+    if origin == "upper":
+        v_origin = 1.0
+    elif origin == "lower":
+        v_origin = -1.0
+    else:
+        raise AssertionError("origin must be 'upper' or 'lower', not {}".format(origin))
+    images = images.to(dtype=torch.float32).contiguous()
+    params = params.to(dtype=torch.float32).contiguous()
+    if images.dim() != 3 or images.shape[1] != images.shape[2]:
+        raise ValueError("images must be (B, nxy, nxy)")
+    if params.dim() != 2 or params.shape != (images.shape[0], 3):
+        raise ValueError("params must be (B, 3): PA, dRA, dDec")
+    if not (images.is_cuda and params.is_cuda):
+        raise ValueError("images and params must be CUDA tensors")
+    B, nxy = images.shape[0], images.shape[1]
+    dev = images.device
+    chi2 = torch.empty(B, dtype=torch.float64, device=dev)
+    sets = torch.empty((B, dataset.nsets), dtype=torch.float64, device=dev) if per_set else None
+    gI = torch.empty_like(images) if grad else None
+    gp = torch.empty_like(params) if grad else None
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    L = _bind()
+    _lib.check(L.galario_chi2_image_batch_f(dataset.handle, B, nxy, images.data_ptr(), _F(dxy), _F(v_origin),
+                                            params.data_ptr(), chi2.data_ptr(),
+                                            sets.data_ptr() if per_set else None,
+                                            gI.data_ptr() if grad else None, gp.data_ptr() if grad else None,
+                                            _P(stream)))
     out = sets if per_set else chi2
     return (out, gI, gp) if grad else out

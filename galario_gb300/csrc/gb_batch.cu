@@ -76,13 +76,17 @@ struct Geo {  // geometry shared by all models of a batch
 // ---------------------------------------------------------------------------
 // forward kernels
 // ---------------------------------------------------------------------------
-__global__ void model_setup_kernel(int B, const float* __restrict__ params, const float* __restrict__ intensity,
-                                   int nr, const double* __restrict__ central_coef, int ncoef, double inv_duv,
+// params per model: (inc, PA, dRA, dDec) for profiles (pstride 4), (PA, dRA,
+// dDec) for images (pstride 3, no inclination)
+__global__ void model_setup_kernel(int B, const float* __restrict__ params, int pstride,
+                                   const float* __restrict__ intensity, int nr,
+                                   const double* __restrict__ central_coef, int ncoef, double inv_duv,
                                    ModelConst* mc) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
-    const double inc = params[4 * b + 0], PA = params[4 * b + 1];
-    const double dRA = params[4 * b + 2], dDec = params[4 * b + 3];
+    const float* pb = params + (size_t)pstride * b + (pstride - 3);
+    const double inc = pstride == 4 ? params[(size_t)4 * b] : 0.0;
+    const double PA = pb[0], dRA = pb[1], dDec = pb[2];
     ModelConst m;
     auto split = [](double x) {
         DF r;
@@ -768,14 +772,110 @@ __global__ void central_adjoint_kernel(int B, int nr, const double* __restrict__
     for (int i = threadIdx.x; i < ncoef; i += blockDim.x) gI[(size_t)b * nr + i] += (float)(coef[i] * gcentral[b]);
 }
 
-__global__ void write_grad_params_kernel(int B, const double* __restrict__ gsum, const double* __restrict__ ginc,
-                                         float* __restrict__ gp) {
+__global__ void write_grad_params_kernel(int B, int pstride, const double* __restrict__ gsum,
+                                         const double* __restrict__ ginc, float* __restrict__ gp) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
-    gp[4 * b + 0] = (float)ginc[b];
-    gp[4 * b + 1] = (float)gsum[b * kAcc + 1];
-    gp[4 * b + 2] = (float)gsum[b * kAcc + 2];
-    gp[4 * b + 3] = (float)gsum[b * kAcc + 3];
+    float* o = gp + (size_t)pstride * b;
+    if (pstride == 4) *o++ = (float)ginc[b];
+    o[0] = (float)gsum[b * kAcc + 1];
+    o[1] = (float)gsum[b * kAcc + 2];
+    o[2] = (float)gsum[b * kAcc + 3];
+}
+
+// ---------------------------------------------------------------------------
+// image models: B images of N x N pixels [Jy/pixel], all N rows transformed
+// (band0 = 0, R = N).  A CTA takes F consecutive rows and stages their K
+// spectrum columns in shared memory (row stride S = F + 1) so that the
+// transposed layout zt[b][k][row] is written, and read back by the adjoint,
+// in contiguous runs of F rows.
+// ---------------------------------------------------------------------------
+template <int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) rows_image_batch_kernel(Geo g, int F, const float* __restrict__ images,
+                                                                const float2* __restrict__ tw,
+                                                                const float2* __restrict__ stw,
+                                                                float2* __restrict__ zt) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* buf = reinterpret_cast<float2*>(smem_raw);
+    const int S = F + 1;
+    float2* stg = buf + fft_slots(g.M);  // [K][S]
+    const int b = blockIdx.y;
+    const int i0 = blockIdx.x * F;
+    const int nrow = min(F, g.N - i0);
+    const float* img = images + (size_t)b * g.N * g.N;
+    for (int rr = 0; rr < nrow; ++rr) {
+        const int i = i0 + rr;
+        const float2* row = reinterpret_cast<const float2*>(img + (size_t)i * g.N);
+        __syncthreads();  // buf free
+        for (int mm = threadIdx.x; mm < g.M; mm += blockDim.x) buf[sp(mm)] = __ldg(&row[mm]);
+        __syncthreads();
+        block_fft<float, E>(buf, g.M, ilog2(g.M), stw);
+        const float sgn = (i & 1) ? -1.f : 1.f;  // the image fftshift, folded into the rows
+        for (int k = threadIdx.x; k < g.K; k += blockDim.x) {
+            const float2 x = real_split<float>(buf, g.M, k, tw);
+            stg[k * S + rr] = make_float2(sgn * x.x, sgn * x.y);
+        }
+    }
+    __syncthreads();
+    float2* out = zt + (size_t)b * g.K * g.R;
+    const float inv_n = 1.f / i2f_small(nrow);
+    for (int e = threadIdx.x; e < g.K * nrow; e += blockDim.x) {
+        int k, j;
+        split_index(e, nrow, inv_n, &k, &j);
+        out[(size_t)k * g.R + i0 + j] = stg[k * S + j];
+    }
+}
+
+// adjoint of rows_image_batch_kernel: dchi2/d(pixel) of every image row
+template <int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) rowsT_image_batch_kernel(Geo g, int F, const float2* __restrict__ stw,
+                                                                 const float2* __restrict__ twc,
+                                                                 const float2* __restrict__ zbar,
+                                                                 float* __restrict__ gimg) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* buf = reinterpret_cast<float2*>(smem_raw);
+    const int S = F + 1;
+    float2* stg = buf + fft_slots(g.M);  // [K][S]
+    const int b = blockIdx.y;
+    const int i0 = blockIdx.x * F;
+    const int nrow = min(F, g.N - i0);
+    const int M = g.M;
+    const float2* zb = zbar + (size_t)b * g.K * g.R;
+    {
+        const float inv_n = 1.f / i2f_small(nrow);
+        for (int e = threadIdx.x; e < g.K * nrow; e += blockDim.x) {
+            int k, j;
+            split_index(e, nrow, inv_n, &k, &j);
+            stg[k * S + j] = zb[(size_t)k * g.R + i0 + j];
+        }
+    }
+    for (int rr = 0; rr < nrow; ++rr) {
+        const int i = i0 + rr;
+        __syncthreads();
+        // Hermitian weights: Y~0 = Re Y0, Y~k = Yk/2 (0<k<M), Y~M = Re YM; zero for k >= K
+        for (int k = threadIdx.x; k < M; k += blockDim.x) {
+            auto yk = [&](int kk) -> float2 {
+                if (kk >= g.K) return make_float2(0.f, 0.f);
+                const float2 y = stg[kk * S + rr];
+                if (kk == 0 || kk == M) return make_float2(y.x, 0.f);
+                return make_float2(0.5f * y.x, 0.5f * y.y);
+            };
+            const float2 ya = yk(k), yc = yk(M - k);
+            const float2 Ep = make_float2(ya.x + yc.x, ya.y - yc.y);
+            const float2 d = make_float2(ya.x - yc.x, ya.y + yc.y);
+            const float2 w = twc[k];  // e^{+2 pi i k / N}
+            const float2 Op = make_float2(d.x * w.x - d.y * w.y, d.x * w.y + d.y * w.x);
+            buf[sp(k)] = make_float2(Ep.x - Op.y, -(Ep.y + Op.x));  // conjugated: inverse FFT by a forward one
+        }
+        __syncthreads();
+        block_fft<float, E>(buf, M, ilog2(M), stw);
+        const float sgn = (i & 1) ? -1.f : 1.f;
+        float2* grow = reinterpret_cast<float2*>(gimg + ((size_t)b * g.N + i) * g.N);
+        for (int mm = threadIdx.x; mm < M; mm += blockDim.x) {
+            const float2 zz = buf[sp(mm)];  // conj(z): x[2m] = Re z, x[2m+1] = Im z
+            grow[mm] = make_float2(sgn * zz.x, -sgn * zz.y);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -791,7 +891,7 @@ struct Shape {
     int e_rows, e_cols, e_colsT, e_rowsT, pts;
 };
 struct TuneKey {
-    int N, K, W, R, B, nd, grad, nr;
+    int N, K, W, R, B, nd, grad, nr, image;
     bool operator<(const TuneKey& o) const {
         return std::memcmp(this, &o, sizeof(TuneKey)) < 0;
     }
@@ -885,11 +985,11 @@ struct Buf {
 struct GraphKey {
     TuneKey tk;
     unsigned long long dataset;  // Dataset::serial
-    float Rmin, dR, dxy;
+    float Rmin, dR, dxy, vo;
     int per_set;
     bool operator<(const GraphKey& o) const {
-        return std::tie(tk, dataset, Rmin, dR, dxy, per_set) <
-               std::tie(o.tk, o.dataset, o.Rmin, o.dR, o.dxy, o.per_set);
+        return std::tie(tk, dataset, Rmin, dR, dxy, vo, per_set) <
+               std::tie(o.tk, o.dataset, o.Rmin, o.dR, o.dxy, o.vo, o.per_set);
     }
 };
 struct GraphEntry {
@@ -1231,11 +1331,40 @@ API int galario_dataset_nsets(void* handle, int* nsets) {
     });
 }
 
-API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* intensity, float Rmin, float dR,
-                                     float dxy, int nxy, const float* params, double* chi2, double* chi2_sets,
-                                     float* grad_intensity, float* grad_params, void* stream) {
-    return bguard([&] {
-        Dataset* d = static_cast<Dataset*>(dataset);
+// One batched call: B models (radial profiles or images) against a dataset.
+struct BatchCall {
+    gbg::Dataset* d = nullptr;
+    int B = 0;
+    bool image = false;
+    int nr = 0;                        // profiles: samples per profile
+    const float* input = nullptr;      // profiles (B x nr) or images (B x nxy x nxy)
+    float Rmin = 0.f, dR = 0.f;        // profiles
+    float dxy = 0.f, vo = 1.f;
+    int nxy = 0;
+    const float* params = nullptr;     // B x pstride
+    int pstride = 4;
+    double* chi2 = nullptr;
+    double* chi2_sets = nullptr;
+    float* grad_input = nullptr;
+    float* grad_params = nullptr;
+    void* stream = nullptr;
+};
+
+static void batch_run(const BatchCall& call) {
+        Dataset* d = call.d;
+        const int B = call.B;
+        const bool image = call.image;
+        const int nr = image ? 0 : call.nr;
+        const float* intensity = call.input;  // the model input: profiles or images
+        const float Rmin = call.Rmin, dR = call.dR, dxy = call.dxy;
+        const int nxy = call.nxy;
+        const float* params = call.params;
+        const int pstride = call.pstride;
+        double* chi2 = call.chi2;
+        double* chi2_sets = call.chi2_sets;
+        float* grad_intensity = call.grad_input;
+        float* grad_params = call.grad_params;
+        void* stream = call.stream;
         if (!d) throw Err{GALARIO_EINVAL, "Error in batch: dataset is NULL"};
         if (B <= 0) throw Err{GALARIO_EINVAL, "Error in batch: B must be positive"};
         if (nxy < 2 || (nxy & 1))
@@ -1243,12 +1372,14 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
                                           (nxy < 2 ? " is less than 2" : " is odd")};
         if (!is_pow2(nxy) || nxy < 16 || nxy > 16384)
             throw Err{GALARIO_EINVAL, "Error in batch: nxy must be a power of two in [16, 16384]"};
-        const double ratio = ((double)dxy / 2. - (double)Rmin) / (double)dR;
-        if (ratio < 5)
-            throw Err{GALARIO_EINVAL,
-                      "Error in create image: Expect (dxy/2-Rmin)/dR > 5, i.e. dR small enough to ensure reliable "
-                      "interpolation the inside central pixel but got (dxy/2-Rmin)/dR = " + std::to_string(ratio) +
-                          ". Try reducing dR."};
+        if (!image) {
+            const double ratio = ((double)dxy / 2. - (double)Rmin) / (double)dR;
+            if (ratio < 5)
+                throw Err{GALARIO_EINVAL,
+                          "Error in create image: Expect (dxy/2-Rmin)/dR > 5, i.e. dR small enough to ensure reliable "
+                          "interpolation the inside central pixel but got (dxy/2-Rmin)/dR = " +
+                              std::to_string(ratio) + ". Try reducing dR."};
+        }
         const bool grad = grad_intensity || grad_params;
         if (grad && !(grad_intensity && grad_params))
             throw Err{GALARIO_EINVAL, "Error in batch: pass both gradient outputs or neither"};
@@ -1274,29 +1405,36 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
         g.K = w.K;
         g.r0 = w.r0;
         g.W = w.W;
-        long long rm = (long long)std::ceil(((double)Rmin + nr * (double)dR) / (double)dxy);
-        g.rmax = (int)(rm < nxy / 2 ? rm : nxy / 2);
-        g.band0 = nxy / 2 - g.rmax;
-        g.R = 2 * g.rmax;
+        if (image) {  // every row of the image is transformed
+            g.rmax = nxy / 2;
+            g.band0 = 0;
+            g.R = nxy;
+        } else {
+            long long rm = (long long)std::ceil(((double)Rmin + nr * (double)dR) / (double)dxy);
+            g.rmax = (int)(rm < nxy / 2 ? rm : nxy / 2);
+            g.band0 = nxy / 2 - g.rmax;
+            g.R = 2 * g.rmax;
+        }
         g.nr = nr;
         g.Rmin = Rmin;
         g.dR = dR;
-        g.inv_dR = (float)(1.0 / (double)dR);
+        g.inv_dR = image ? 0.f : (float)(1.0 / (double)dR);
         g.dxy = dxy;
         g.sr_to_px = dxy * dxy;
         const double inv_duv = 1.0 / duv;
         g.inv_duv_hi = (float)inv_duv;
         g.inv_duv_lo = (float)(inv_duv - (double)g.inv_duv_hi);
         g.half_nrow = (float)(nxy / 2);
-        g.vo = 1.f;
+        g.vo = call.vo;
         if (g.R <= 0) throw Err{GALARIO_EINVAL, "Error in batch: empty profile support"};
-        if (nr < 2 || nr >= (1 << 22)) throw Err{GALARIO_EINVAL, "Error in batch: nr out of range"};
-        // central-pixel coefficients: central = sum_i coef_i I_i (reference :1136-1153)
-        const int iIN = (int)std::floor(((double)dxy / 2 - (double)Rmin) / (double)dR);
-        if (iIN < 0 || iIN + 1 >= nr) throw Err{GALARIO_EINVAL, "Error in create image: profile too short"};
+        if (!image && (nr < 2 || nr >= (1 << 22))) throw Err{GALARIO_EINVAL, "Error in batch: nr out of range"};
+        // central-pixel coefficients of profiles: central = sum_i coef_i I_i (reference :1136-1153)
+        const int iIN = image ? 0 : (int)std::floor(((double)dxy / 2 - (double)Rmin) / (double)dR);
+        if (!image && (iIN < 0 || iIN + 1 >= nr))
+            throw Err{GALARIO_EINVAL, "Error in create image: profile too short"};
         g.iIN = iIN;
-        std::vector<double> coef((size_t)iIN + 2, 0.0);
-        {
+        std::vector<double> coef(image ? 0 : (size_t)iIN + 2, 0.0);
+        if (!image) {
             const double Rm = Rmin, dr = dR, h = (double)dxy / 2.;
             for (int i = 1; i < iIN; ++i) coef[i] += 2. * dr * (Rm + dr * i);
             coef[0] += dr * Rm;
@@ -1310,7 +1448,7 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
             const double sr = (double)dxy * (double)dxy;
             for (auto& c : coef) c *= sr / area;
         }
-        const int ncoef = iIN + 2;
+        const int ncoef = image ? 0 : iIN + 2;
 
         // ---- buffers ----
         const long long ncell = (long long)g.K * g.W;
@@ -1324,7 +1462,7 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
         double* partials = ws.partials.get<double>((size_t)max_vblocks * B * kAcc);
         double* gsum = ws.gsum.get<double>((size_t)B * kAcc);
         auto tws = ws.twiddles(nxy);
-        BCK(cudaMemcpyAsync(coef_d, coef.data(), sizeof(double) * ncoef, cudaMemcpyHostToDevice, s));
+        if (ncoef) BCK(cudaMemcpyAsync(coef_d, coef.data(), sizeof(double) * ncoef, cudaMemcpyHostToDevice, s));
         DevState* st = ws.state.get<DevState>(1);
         BCK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
         float* cgrad = grad ? ws.cgrad.get<float>((size_t)B * ncell * kGRec) : nullptr;
@@ -1346,9 +1484,27 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
         const int GrowsT = std::max(1, kRowsPerCta / Frows);
         // ---- launchers, one per pass, parameterised by the tuned shape ----
         auto fft_threads = [](int L, int E) { return L / E; };
+        auto check_smem = [](size_t sm) {
+            if (sm > 227 * 1024)
+                throw Err{GALARIO_EINVAL, "Error in batch: nxy and the uv coverage need " + std::to_string(sm) +
+                                              " bytes of shared memory per block (at most 232448)"};
+        };
+        const int Fimg = 2 * Frows;  // image rows per CTA of the image row passes
         auto rows = [&](int E) {
+            if (image) {
+                const size_t sm = sizeof(float2) * (fft_slots(g.M) + (size_t)g.K * (Fimg + 1));
+                check_smem(sm);
+                GBB_DISPATCH_E(E, fft_threads(g.M, E), {
+                    BCK((cudaError_t)smem_attr((const void*)rows_image_batch_kernel<EE, TT>, sm));
+                    rows_image_batch_kernel<EE, TT><<<dim3((g.N + Fimg - 1) / Fimg, B), fft_threads(g.M, EE), sm, s>>>(
+                        g, Fimg, intensity, tws.first, ws.stage_tw(g.M, EE), zt);
+                });
+                BCK(cudaGetLastError());
+                return;
+            }
             const size_t sm = sizeof(float2) * (fft_slots(g.M) + (size_t)g.K * (2 * Frows + 1)) +
                               sizeof(float) * (g.rmax + 1);
+            check_smem(sm);
             GBB_DISPATCH_E(E, fft_threads(g.M, E), {
                 BCK((cudaError_t)smem_attr((const void*)rows_batch_kernel<EE, TT>, sm));
                 rows_batch_kernel<EE, TT><<<dim3((g.rmax + Frows) / Frows, B), fft_threads(g.M, EE), sm, s>>>(
@@ -1396,9 +1552,20 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
             BCK(cudaGetLastError());
         };
         auto rowsT = [&](int E) {
+            if (image) {
+                const size_t smi = sizeof(float2) * (fft_slots(g.M) + (size_t)g.K * (Fimg + 1));
+                check_smem(smi);
+                GBB_DISPATCH_E(E, fft_threads(g.M, E), {
+                    BCK((cudaError_t)smem_attr((const void*)rowsT_image_batch_kernel<EE, TT>, smi));
+                    rowsT_image_batch_kernel<EE, TT><<<dim3((g.N + Fimg - 1) / Fimg, B), fft_threads(g.M, EE), smi, s>>>(
+                        g, Fimg, ws.stage_tw(g.M, EE), tws.second, zbar, grad_intensity);
+                });
+                BCK(cudaGetLastError());
+                return;
+            }
             const size_t sm = sizeof(float2) * (fft_slots(g.M) + (size_t)g.K * (2 * Frows + 1)) +
                               sizeof(float) * (nr + g.rmax + 1);
-            if (sm > 220 * 1024) throw Err{GALARIO_EINVAL, "Error in batch: nxy/nr too large for the row adjoint"};
+            check_smem(sm);
             GBB_DISPATCH_E(E, fft_threads(g.M, E), {
                 BCK((cudaError_t)smem_attr((const void*)rowsT_batch_kernel<EE, TT>, sm));
                 rowsT_batch_kernel<EE, TT><<<dim3((g.rmax + Frows * GrowsT) / (Frows * GrowsT), B), fft_threads(g.M, EE), sm, s>>>(
@@ -1410,18 +1577,19 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
             BCK(cudaMemsetAsync(cgrad, 0, sizeof(float) * (size_t)B * ncell * kGRec, s));
             BCK(cudaMemsetAsync(ginc_d, 0, sizeof(double) * B, s));
             BCK(cudaMemsetAsync(gcentral, 0, sizeof(float) * B, s));
-            BCK(cudaMemsetAsync(grad_intensity, 0, sizeof(float) * (size_t)B * nr, s));
+            if (!image) BCK(cudaMemsetAsync(grad_intensity, 0, sizeof(float) * (size_t)B * nr, s));
         };
 
         // ---- launch shapes: tuned once per geometry ----
         Shape sh = default_shape(g);
-        const TuneKey key{g.N, g.K, g.W, g.R, B, d->nd_pad, grad ? 1 : 0, nr};
+        const TuneKey key{g.N, g.K, g.W, g.R, B, d->nd_pad, grad ? 1 : 0, nr, image ? 1 : 0};
         auto it = ws.shapes.find(key);
         if (it != ws.shapes.end()) {
             sh = it->second;
         } else if (autotune_enabled()) {
             // valid inputs for every pass, then each candidate timed in isolation
-            model_setup_kernel<<<(B + 31) / 32, 32, 0, s>>>(B, params, intensity, nr, coef_d, ncoef, inv_duv, mc);
+            model_setup_kernel<<<(B + 31) / 32, 32, 0, s>>>(B, params, pstride, intensity, nr, coef_d, ncoef, inv_duv,
+                                                             mc);
             BCK(cudaGetLastError());
             rows(sh.e_rows);
             cols(sh.e_cols);
@@ -1445,7 +1613,8 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
         // ---- the launch sequence of one call ----
         auto run_all = [&] {
             BCK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
-            model_setup_kernel<<<(B + 31) / 32, 32, 0, s>>>(B, params, intensity, nr, coef_d, ncoef, inv_duv, mc);
+            model_setup_kernel<<<(B + 31) / 32, 32, 0, s>>>(B, params, pstride, intensity, nr, coef_d, ncoef, inv_duv,
+                                                             mc);
             BCK(cudaGetLastError());
             rows(sh.e_rows);
             cols(sh.e_cols);
@@ -1462,16 +1631,18 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
             BCK(cudaGetLastError());
             colsT(sh.e_colsT);
             rowsT(sh.e_rowsT);
-            central_adjoint_kernel<<<B, 64, 0, s>>>(B, nr, coef_d, ncoef, gcentral, grad_intensity);
-            BCK(cudaGetLastError());
-            write_grad_params_kernel<<<(B + 127) / 128, 128, 0, s>>>(B, gsum, ginc_d, grad_params);
+            if (!image) {
+                central_adjoint_kernel<<<B, 64, 0, s>>>(B, nr, coef_d, ncoef, gcentral, grad_intensity);
+                BCK(cudaGetLastError());
+            }
+            write_grad_params_kernel<<<(B + 127) / 128, 128, 0, s>>>(B, pstride, gsum, ginc_d, grad_params);
             BCK(cudaGetLastError());
         };
 
         // First call of a combination: eager (it also sets the kernels'
         // attributes and creates the tables); from the second on, one
         // captured CUDA graph per combination, fed through staging buffers.
-        const GraphKey gk{key, d->serial, Rmin, dR, dxy, chi2_sets ? 1 : 0};
+        const GraphKey gk{key, d->serial, Rmin, dR, dxy, g.vo, chi2_sets ? 1 : 0};
         GraphEntry* ge = nullptr;
         if (graphs_enabled()) {
             auto git = ws.graphs.find(gk);
@@ -1485,7 +1656,8 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
             run_all();
             return;
         }
-        const size_t nI = (size_t)B * nr, nP = (size_t)B * 4, nS = (size_t)B * d->nsets;
+        const size_t nI = (size_t)B * (image ? (size_t)nxy * nxy : (size_t)nr), nP = (size_t)B * pstride;
+        const size_t nS = (size_t)B * d->nsets;
         float* in_I = ws.in_I.get<float>(nI);
         float* in_p = ws.in_p.get<float>(nP);
         double* o_chi2 = ws.out_chi2.get<double>((size_t)B);
@@ -1537,5 +1709,54 @@ API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* 
             BCK(cudaMemcpyAsync(user_gI, o_gI, sizeof(float) * nI, cudaMemcpyDeviceToDevice, s_user));
             BCK(cudaMemcpyAsync(user_gp, o_gp, sizeof(float) * nP, cudaMemcpyDeviceToDevice, s_user));
         }
+}
+
+API int galario_chi2_profile_batch_f(void* dataset, int B, int nr, const float* intensity, float Rmin, float dR,
+                                     float dxy, int nxy, const float* params, double* chi2, double* chi2_sets,
+                                     float* grad_intensity, float* grad_params, void* stream) {
+    return bguard([&] {
+        BatchCall c;
+        c.d = static_cast<Dataset*>(dataset);
+        c.B = B;
+        c.nr = nr;
+        c.input = intensity;
+        c.Rmin = Rmin;
+        c.dR = dR;
+        c.dxy = dxy;
+        c.nxy = nxy;
+        c.vo = 1.f;  // profiles: origin 'upper' (reference src/galario.cpp:1411)
+        c.params = params;
+        c.pstride = 4;
+        c.chi2 = chi2;
+        c.chi2_sets = chi2_sets;
+        c.grad_input = grad_intensity;
+        c.grad_params = grad_params;
+        c.stream = stream;
+        batch_run(c);
+    });
+}
+
+API int galario_chi2_image_batch_f(void* dataset, int B, int nxy, const float* images, float dxy, float v_origin,
+                                   const float* params, double* chi2, double* chi2_sets, float* grad_images,
+                                   float* grad_params, void* stream) {
+    return bguard([&] {
+        if (!(v_origin == 1.f || v_origin == -1.f))
+            throw Err{GALARIO_EINVAL, "Error in batch: v_origin must be +1 ('upper') or -1 ('lower')"};
+        BatchCall c;
+        c.d = static_cast<Dataset*>(dataset);
+        c.B = B;
+        c.image = true;
+        c.input = images;
+        c.dxy = dxy;
+        c.nxy = nxy;
+        c.vo = v_origin;
+        c.params = params;
+        c.pstride = 3;
+        c.chi2 = chi2;
+        c.chi2_sets = chi2_sets;
+        c.grad_input = grad_images;
+        c.grad_params = grad_params;
+        c.stream = stream;
+        batch_run(c);
     });
 }

@@ -229,6 +229,17 @@ int galario_chi2_profile_batch_f(void *dataset, int B, int nr, const float *inte
                                  float dxy, int nxy, const float *params, double *chi2, double *chi2_sets,
                                  float *grad_intensity, float *grad_params, void *stream);
 
+/* chi2 of B images against a dataset (chi2Image semantics per image, no
+ * reference counterpart for the batch or the gradient).  Device pointers:
+ *  images (B x nxy x nxy) [Jy/pixel], nxy a power of two in [16, 16384];
+ *  params (B x 3): PA, dRA, dDec [rad] per image;
+ *  v_origin: +1 ('upper') or -1 ('lower'), as the reference's origin;
+ *  chi2, chi2_sets as galario_chi2_profile_batch_f;
+ *  grad_images (B x nxy x nxy) and grad_params (B x 3), both or neither. */
+int galario_chi2_image_batch_f(void *dataset, int B, int nxy, const float *images, float dxy, float v_origin,
+                               const float *params, double *chi2, double *chi2_sets, float *grad_images,
+                               float *grad_params, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
