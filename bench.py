@@ -20,6 +20,16 @@ the max over ranks and `value` counts the evaluations of all ranks.
   roofline     dominant kernel: algorithmic bytes / mean CUDA-event duration
   cpu_baseline the CPU oracle (C restatement of the reference CPU path) timed
                on a bounded sample on this host's cores
+  batched      B=64 models of the workload, FP32 with double-float index and
+               phase, chi2 and the gradient w.r.t. every profile sample and
+               (inc, PA, dRA, dDec), one call per step (galario_gb300.batch)
+  batched_sets B=256 single-ring profiles against 8 uneven visibility sets
+               (nxy=2048), chi2 per set, with and without the gradient
+  batched_images B=16 free-form 2048^2 images against the same 8 sets, chi2
+               and the gradient w.r.t. every pixel and (PA, dRA, dDec)
+--part plain|batched
+  run only the plain (FP64/FP32 single-model) or only the batched
+  measurements and print their own JSON line (for profiling runs)
 --impl reference
   the reference's CPU implementation of the path (the reference build in
   oracle/_ref when present, else the C restatement oracle/_build), on all
@@ -340,8 +350,18 @@ def run_ours(args):
                   if cnt[i]}
         return ms, stages, float(chi2_d.item()), clk.summary(), wall
 
-    ms64, stages64, chi2_64, clocks, wall64 = device_rate("double")
-    ms32, stages32, chi2_32, _, _ = device_rate("single")
+    if args.part == "batched":  # profiling runs of the batched path: the FP64 chi2 from one public call
+        chi2_64 = g.double.chi2Profile(wl.intensity, wl.Rmin, wl.dR, wl.nxy, wl.dxy, wl.u, wl.v, re, im, wl.w,
+                                       **wl.kw())
+    else:
+        ms64, stages64, chi2_64, clocks, wall64 = device_rate("double")
+        ms32, stages32, chi2_32, _, _ = device_rate("single")
+    if args.part == "plain":
+        if rank == 0:
+            print(json.dumps({"part": "plain", "f64_evals_per_s": world * args.steps / (ms64 / 1e3),
+                              "f32_evals_per_s": world * args.steps / (ms32 / 1e3), "stages_f64": stages64,
+                              "stages_f32": stages32}), flush=True)
+        return 0
 
     # batched FP32 + gradient: B models (model 0 = the workload's parameters,
     # the others perturbed) on the same dataset, every step computes the B
@@ -381,7 +401,88 @@ def run_ours(args):
                 "ms_per_step": ms / steps, "rel_chi2_vs_f64": abs(chi2_b0 - chi2_64) / abs(chi2_64),
                 "gpu_launches_per_step": 11}
 
+    # the multi-dataset workload: B single-ring profiles, nxy=2048, dxy=5e-3",
+    # Rmin=1e-4", dR=4e-4", nr=4096; 8 visibility sets with nd_k ~ U[2e5, 3e6],
+    # radius log-uniform in [1e4, 2e6] wavelengths, seed 1000 + k
+    def sets_workload():
+        sets = []
+        for k in range(8):
+            r = np.random.default_rng(1000 + k)
+            n = int(r.uniform(2e5, 3e6))
+            rad = np.exp(r.uniform(np.log(1e4), np.log(2e6), n))
+            th = r.uniform(0, 2 * np.pi, n)
+            sig = r.uniform(0.5e-3, 1.5e-3, n)
+            sets.append((rad * np.cos(th), rad * np.sin(th), r.normal(0, sig), r.normal(0, sig), 1 / sig ** 2))
+        return sets
+
+    def timed(fn, steps):
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                flush.zero_()
+                out = fn()
+            torch.cuda.synchronize()
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            for a, b in evs:
+                flush.zero_()
+                a.record(stream)
+                out = fn()
+                b.record(stream)
+            torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in evs), out
+
+    def batched_sets_rate(ds, B=256):
+        from galario_gb300.batch import chi2_profile_batch
+        nxy, dxy, Rmin, dR, nr = 2048, 5e-3 * ARCSEC, 1e-4 * ARCSEC, 4e-4 * ARCSEC, 4096
+        r = np.random.default_rng(7)
+        R = Rmin + dR * np.arange(nr)
+        r0, sig = r.uniform(0.1, 0.8, B) * ARCSEC, r.uniform(0.01, 0.1, B) * ARCSEC
+        flux = r.uniform(0.05, 0.2, B)
+        prof = np.exp(-0.5 * ((R[None, :] - r0[:, None]) / sig[:, None]) ** 2)
+        prof *= (flux / (2 * np.pi * (prof * R[None, :]).sum(axis=1) * dR))[:, None]  # Jy/sr
+        prm = np.c_[r.uniform(0, 70, B) * DEG, r.uniform(0, 180, B) * DEG, np.zeros(B), np.zeros(B)]
+        tI = torch.tensor(prof, dtype=torch.float32, device=dev)
+        tp = torch.tensor(prm, dtype=torch.float32, device=dev)
+        steps = max(3, args.steps // 60)
+        out = {"B": B, "nsets": ds.nsets, "nvis": ds.nd, "nxy": nxy, "steps": steps, "unit": UNIT}
+        for grad in (False, True):
+            ms, _ = timed(lambda: chi2_profile_batch(ds, tI, tp, Rmin, dR, dxy, nxy, grad=grad, per_set=True),
+                          steps)
+            out["grad" if grad else "forward"] = {"value": B * steps / (ms * 1e-3), "ms_per_step": ms / steps}
+        return out
+
+    def batched_images_rate(ds, B=16):
+        from galario_gb300.batch import chi2_image_batch
+        nxy, dxy = 2048, 5e-3 * ARCSEC
+        r = np.random.default_rng(8)
+        x = (np.arange(nxy) - nxy / 2) * dxy
+        X, Y = np.meshgrid(x, x)
+        rad = np.hypot(X, Y)
+        imgs = torch.empty((B, nxy, nxy), dtype=torch.float32, device=dev)
+        for b in range(B):
+            ring = np.exp(-0.5 * ((rad - r.uniform(0.2, 0.8) * ARCSEC) / (r.uniform(0.03, 0.1) * ARCSEC)) ** 2)
+            ring += r.normal(0, 1e-4, ring.shape)
+            imgs[b] = torch.from_numpy(ring * (0.1 / ring.sum()))
+        tp = torch.tensor(np.c_[r.uniform(0, np.pi, B), r.uniform(-0.05, 0.05, (B, 2)) * ARCSEC],
+                          dtype=torch.float32, device=dev)
+        steps = max(3, args.steps // 60)
+        ms, _ = timed(lambda: chi2_image_batch(ds, imgs, tp, dxy, grad=True), steps)
+        return {"value": B * steps / (ms * 1e-3), "unit": UNIT, "B": B, "nxy": nxy, "nsets": ds.nsets,
+                "nvis": ds.nd, "ms_per_step": ms / steps, "steps": steps,
+                "gradient": "chi2 and dchi2/d(every pixel, PA, dRA, dDec) per image"}
+
     batched = batched_rate()
+    from galario_gb300.batch import Dataset as _Dataset
+    _sets = sets_workload()
+    ds_sets = _Dataset(*[[st[i] for st in _sets] for i in range(5)])
+    del _sets
+    batched_sets = batched_sets_rate(ds_sets)
+    batched_images = batched_images_rate(ds_sets)
+    ds_sets.close()
+    if args.part == "batched":
+        if rank == 0:
+            print(json.dumps({"part": "batched", "batched": batched, "batched_sets": batched_sets,
+                              "batched_images": batched_images}), flush=True)
+        return 0
 
     # max over ranks of the timed region
     t_local = ms64 / 1e3
@@ -452,6 +553,8 @@ def run_ours(args):
                        "rel_chi2_vs_f64": abs(chi2_32 - chi2_64) / abs(chi2_64),
                        "vis_GBs": alg32["vis"] / (stages32.get("vis", 1e9) * 1e-3) / 1e9},
             "batched": dict(batched, ratio_vs_plain_f64=batched["value"] / value),
+            "batched_sets": batched_sets,
+            "batched_images": batched_images,
             "cpu_baseline": {"value": rate_cpu, "unit": UNIT, "cores": cores, "kind": kind,
                              "sample": "2 full chi2Profile evaluations (FP64, FFT from the project's C FFT in place "
                                        "of FFTW), first call dropped"},
@@ -473,6 +576,7 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--part", choices=["all", "plain", "batched"], default="all")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

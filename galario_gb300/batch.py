@@ -33,13 +33,22 @@ def _bind():
         L.galario_dataset_free.argtypes = [_P]
         L.galario_dataset_nvis.argtypes = [_P, C.POINTER(_I)]
         L.galario_dataset_nsets.argtypes = [_P, C.POINTER(_I)]
+        L.galario_batch_status.argtypes = [C.POINTER(C.c_uint)]
         L.galario_chi2_profile_batch_f.argtypes = [_P, _I, _I, _P, _F, _F, _F, _I, _P, _P, _P, _P, _P, _P]
         L.galario_chi2_image_batch_f.argtypes = [_P, _I, _I, _P, _F, _F, _P, _P, _P, _P, _P, _P]
         for n in ("galario_dataset_create_f", "galario_dataset_free", "galario_dataset_nvis",
-                  "galario_dataset_nsets", "galario_chi2_profile_batch_f", "galario_chi2_image_batch_f"):
+                  "galario_dataset_nsets", "galario_chi2_profile_batch_f", "galario_chi2_image_batch_f",
+                  "galario_batch_status"):
             getattr(L, n).restype = _I
         L._gb_batch_bound = True
     return L
+
+
+def status() -> int:
+    """Synchronise the device and return the error bits of the last batched call (0: none)."""
+    e = C.c_uint(0)
+    _lib.check(_bind().galario_batch_status(C.byref(e)))
+    return int(e.value)
 
 
 class Dataset:

@@ -285,54 +285,53 @@ struct PointEval {
     float A, zr, zi, rn;   // interpolated modulus, complex bilinear, 1/|z|
     float pc, ps;          // phase factor
     float ur, vr;          // rotated u, v (float)
-    long long cell;        // cell index in the model's window, -1 if none
+    int cell;              // cell index in the model's window
     unsigned err;
 };
 
+// a*x + b*y for exact floats x, y and double-float a, b, as an unnormalised
+// pair (s, e): s + e equals the product sum to ~2^-44 relative; |e| is a few
+// ulps of s, which is all df_floor needs.
+__device__ __forceinline__ DF df_dot2(float x, DF a, float y, DF b) {
+    const float p1 = __fmul_rn(x, a.hi);
+    const float e1 = __fmaf_rn(x, a.lo, __fmaf_rn(x, a.hi, -p1));
+    const float p2 = __fmul_rn(y, b.hi);
+    const float e2 = __fmaf_rn(y, b.lo, __fmaf_rn(y, b.hi, -p2));
+    const DF s = df_two_sum(p1, p2);
+    return DF{s.hi, __fadd_rn(s.lo, __fadd_rn(e1, e2))};
+}
+
+// Every visibility of a dataset lies inside the spectrum window: the host
+// checks max|uv| against the image's uv range before the launch and the
+// window is derived from the same maximum (with a rounding margin), and the
+// dataset holds only finite (u, v).  The cell indices are still clamped to
+// the window, so that no access can leave it; a clamp that changes an index
+// raises ERR_WINDOW.
 __device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, const float* __restrict__ quads_b,
                                            float u, float v, PointEval& p) {
-    p.V = make_float2(0.f, 0.f);
-    p.cell = -1;
     p.err = 0u;
-    if (!(isfinite(u) && isfinite(v))) {
-        p.err = ERR_UV_NONFINITE;
-        return;
-    }
-    // rotated coordinates in grid units, double-float: a = u'/duv, c = v'/duv
-    const DF a = df_add(df_mul_f(u, m.cu), df_neg(df_mul_f(v, m.sv)));
-    const DF cv = df_add(df_mul_f(u, m.sv), df_mul_f(v, m.cu));
+    // rotated coordinates in grid units: a = u'/duv, c = v'/duv
+    const DF a = df_dot2(u, m.cu, -v, m.sv);
+    const DF cv = df_dot2(u, m.sv, v, m.cu);
     p.ur = a.hi;
     p.vr = cv.hi;
-    const float su = copysignf(1.f, a.hi);
+    const bool neg = a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f);
+    const float su = neg ? -1.f : 1.f;
     p.su = su;
-    const DF indu = a.hi < 0.f ? df_neg(a) : a;
-    const DF indv = df_add(DF{g.half_nrow, 0.f}, (g.vo * su < 0.f) ? df_neg(cv) : cv);
-    const float lim = 8.f * g.half_nrow;
-    if (!(indu.hi < lim && indv.hi > -lim && indv.hi < lim)) {
-        p.err = ERR_UV_OUTSIDE;
-        return;
-    }
+    const DF indu = neg ? df_neg(a) : a;
+    // N/2 + vo su c with |c| < N/2: Fast2Sum
+    const bool flip = g.vo * su < 0.f;
+    const float cs = flip ? -cv.hi : cv.hi, cl = flip ? -cv.lo : cv.lo;
+    const float vh = __fadd_rn(g.half_nrow, cs);
+    const DF indv{vh, __fadd_rn(__fsub_rn(cs, __fsub_rn(vh, g.half_nrow)), cl)};
     int fu, fv;
     df_floor(indu, &fu, &p.q);
     df_floor(indv, &fv, &p.t);
-    int r0 = fv, c0 = fu;
-    while (c0 >= g.C) {
-        c0 -= g.C;
-        r0 += 1;
-    }
-    const bool wrap = (c0 + 1 == g.C);
-    if (r0 < 0 || (wrap ? r0 + 2 : r0 + 1) >= g.N) {
-        p.err = ERR_UV_OUTSIDE;
-        return;
-    }
-    const int qq = r0 - g.r0;
-    const bool inside = wrap ? (g.K == g.C && qq >= 0 && qq < g.W - 2) : (c0 < g.K - 1 && qq >= 0 && qq < g.W - 1);
-    if (!inside) {
-        p.err = ERR_WINDOW;
-        return;
-    }
-    p.cell = (long long)c0 * g.W + qq;
-    const float4* rec = reinterpret_cast<const float4*>(quads_b + p.cell * kRec);
+    const int qq = fv - g.r0;
+    const int c0c = min(max(fu, 0), g.K - 2), qqc = min(max(qq, 0), g.W - 2);
+    if (c0c != fu || qqc != qq) p.err = ERR_WINDOW;
+    p.cell = c0c * g.W + qqc;
+    const float4* rec = reinterpret_cast<const float4*>(quads_b + (size_t)p.cell * kRec);
     const float4 p0 = __ldg(rec), p1 = __ldg(rec + 1), p2 = __ldg(rec + 2);
     p.y[0] = make_float2(p0.x, p0.y);
     p.y[1] = make_float2(p0.z, p0.w);
@@ -364,7 +363,7 @@ __device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, co
     p.ps = 0.f;
     if (m.phase) {
         // u'dRA' + v'dDec' = u dRA + v dDec (both pairs rotated by PA)
-        const DF ph = df_add(df_mul_f(u, m.dra), df_mul_f(v, m.ddec));
+        const DF ph = df_dot2(u, m.dra, v, m.ddec);
         float n;
         if (fabsf(ph.hi) < 4194304.f) rint_i(ph.hi, &n);
         else n = rintf(ph.hi);
@@ -479,8 +478,8 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
                 // visibilities of the spatially sorted dataset, so near the uv
                 // centre many of them hit the same cell: runs of equal cells are
                 // reduced with shuffles first and one lane per run adds atomically.
-                const long long key = has ? p.cell : -1 - (long long)lane;
-                const long long prev = __shfl_up_sync(0xffffffffu, key, 1);
+                const int key = has ? p.cell : -1 - lane;
+                const int prev = __shfl_up_sync(0xffffffffu, key, 1);
                 const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || key != prev);
                 if (heads != 0xffffffffu) {
                     const int seg = __popc(heads & ((2u << lane) - 1u));
@@ -1321,6 +1320,19 @@ API int galario_dataset_nvis(void* handle, int* nd) {
     return bguard([&] {
         if (!handle) throw Err{GALARIO_EINVAL, "Error in dataset: handle is NULL"};
         *nd = static_cast<Dataset*>(handle)->nd;
+    });
+}
+
+API int galario_batch_status(unsigned int* err_bits) {
+    return bguard([&] {
+        if (!err_bits) throw Err{GALARIO_EINVAL, "Error in batch: err_bits is NULL"};
+        BatchWs& ws = batch_ws();
+        std::lock_guard<std::mutex> lk(ws.mu);
+        BCK(cudaDeviceSynchronize());
+        DevState* st = ws.state.get<DevState>(1);
+        unsigned int e = 0;
+        BCK(cudaMemcpy(&e, &st->err, sizeof(unsigned int), cudaMemcpyDeviceToHost));
+        *err_bits = e;
     });
 }
 

@@ -240,6 +240,12 @@ int galario_chi2_image_batch_f(void *dataset, int B, int nxy, const float *image
                                const float *params, double *chi2, double *chi2_sets, float *grad_images,
                                float *grad_params, void *stream);
 
+/* Synchronise the device and return the error bits of the last batched call
+ * on the current device: 0, or 4 when a visibility's cell had to be clamped
+ * to the spectrum window (the host-side checks of the dataset and of the
+ * image's uv range rule this out). */
+int galario_batch_status(unsigned int *err_bits);
+
 #ifdef __cplusplus
 }
 #endif

@@ -76,7 +76,9 @@ def test_batch_chi2_matches_oracle_and_single(case, oracle_port):
     import galario_gb300 as g
     from galario_gb300.batch import chi2_profile_batch
     c = case
+    from galario_gb300.batch import status
     chi2 = chi2_profile_batch(c["ds"], c["tI"], c["tp"], c["Rmin"], c["dR"], c["dxy"], c["nxy"]).cpu().numpy()
+    assert status() == 0  # every visibility inside the spectrum window
     orc = oracle_port.get("port", "double")
     f = np.float32
     for b in range(len(chi2)):

@@ -70,7 +70,9 @@ def icase():
 def test_image_batch_chi2_matches_oracle(icase, oracle_port, origin):
     from galario_gb300.batch import chi2_image_batch
     c = icase
+    from galario_gb300.batch import status
     chi2 = chi2_image_batch(c["ds"], c["tI"], c["tp"], c["dxy"], origin=origin).cpu().numpy()
+    assert status() == 0
     orc = oracle_port.get("port", "double")
     for b in range(len(chi2)):
         PA, dRA, dDec = c["params"][b]
