@@ -69,7 +69,7 @@ def _synthetic_table(path):
     nxy, dxy = 512, 0.01 * arcsec
     duv = 1 / (nxy * dxy)
     u, v = uv_log_uniform(20000, 0.5 * duv, 0.4 * nxy / 2 * duv, seed=5)
-    Rmin, dR, nR = 1e-4 * arcsec, 1e-3 * arcsec, 2000
+    Rmin, dR, nR = 1e-4 * arcsec, 5e-4 * arcsec, 4000  # (dxy/2 - Rmin)/dR = 9.8 >= 5
     R = Rmin + dR * np.arange(nR)
     truth = np.array([10.3, 0.4, 35.0, 60.0, 0.05, -0.08])
     I = 10 ** truth[0] * np.exp(-0.5 * (R / (truth[1] * arcsec)) ** 2)
