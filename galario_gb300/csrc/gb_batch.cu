@@ -141,7 +141,7 @@ __device__ __forceinline__ int fold_rows(const Geo& g, int a0, int F, int* lo0, 
     return n0;
 }
 
-template <int E, int MAXT>
+template <int E, int MAXT, int LG>
 __global__ void __launch_bounds__(MAXT) rows_batch_kernel(Geo g, int F, const float* __restrict__ intensity,
                                                           const ModelConst* __restrict__ mc,
                                                           const float2* __restrict__ tw,
@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(MAXT) rows_batch_kernel(Geo g, int F, const fl
                 buf[sp(mm)] = make_float2(x0, x1);
             }
             __syncthreads();
-            block_fft<float, E>(buf, g.M, ilog2(g.M), stw);
+            block_fft_sel<float, E, LG>(buf, g.M, stw);
             const float sgn = (I & 1) ? -1.f : 1.f;
             for (int k = threadIdx.x; k < g.K; k += blockDim.x) {
                 const float2 x = real_split<float>(buf, g.M, k, tw);
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(MAXT) rows_batch_kernel(Geo g, int F, const fl
     }
 }
 
-template <int E, int MAXT>
+template <int E, int MAXT, int LG>
 __global__ void __launch_bounds__(MAXT) cols_batch_kernel(Geo g, const float2* __restrict__ zt,
                                                           const float2* __restrict__ stw, float2* __restrict__ win,
                                                           float* __restrict__ amp) {
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(MAXT) cols_batch_kernel(Geo g, const float2* _
         buf[sp(i)] = (q >= 0 && q < g.R) ? __ldg(&col[q]) : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    block_fft<float, E>(buf, g.N, ilog2(g.N), stw);
+    block_fft_sel<float, E, LG>(buf, g.N, stw);
     const int par = (k + g.N / 2) & 1;
     float2* wcol = win + ((size_t)b * g.K + k) * g.W;
     float* acol = amp + ((size_t)b * g.K + k) * g.W;
@@ -603,7 +603,7 @@ __global__ void quadT_batch_kernel(Geo g, int B, const float* __restrict__ cgrad
 // adjoint of the column pass: inverse column FFT of the window gradient, kept
 // on the band rows.  IFFT(x) = conj(FFT(conj(x))): the forward transform runs
 // on the conjugated column.
-template <int E, int MAXT>
+template <int E, int MAXT, int LG>
 __global__ void __launch_bounds__(MAXT) colsT_batch_kernel(Geo g, const float2* __restrict__ gwin,
                                                            const float2* __restrict__ stw,
                                                            float2* __restrict__ zbar) {
@@ -617,7 +617,7 @@ __global__ void __launch_bounds__(MAXT) colsT_batch_kernel(Geo g, const float2* 
         buf[sp(i)] = make_float2(x.x, -x.y);
     }
     __syncthreads();
-    block_fft<float, E>(buf, g.N, ilog2(g.N), stw);
+    block_fft_sel<float, E, LG>(buf, g.N, stw);
     float2* out = zbar + ((size_t)b * g.K + k) * g.R;
     for (int q = threadIdx.x; q < g.R; q += blockDim.x) {
         const float2 x = buf[sp(g.band0 + q)];
@@ -629,7 +629,7 @@ __global__ void __launch_bounds__(MAXT) colsT_batch_kernel(Geo g, const float2* 
 // (-1)^I Re(sum_{k<K} zbar[k] e^{+2 pi i j k/N}) via the half-length inverse
 // complex FFT (Hermitian weights), then the sweep adjoint into the profile
 // and the inclination.
-template <int E, int MAXT>
+template <int E, int MAXT, int LG>
 __global__ void __launch_bounds__(MAXT) rowsT_batch_kernel(Geo g, int F, int G, const float* __restrict__ intensity,
                                                            const ModelConst* __restrict__ mc,
                                                            const float2* __restrict__ stw,
@@ -707,7 +707,7 @@ __global__ void __launch_bounds__(MAXT) rowsT_batch_kernel(Geo g, int F, int G, 
                 buf[sp(k)] = make_float2(Ep.x - Op.y, -(Ep.y + Op.x));
             }
             __syncthreads();
-            block_fft<float, E>(buf, M, ilog2(M), stw);
+            block_fft_sel<float, E, LG>(buf, M, stw);
             const float sgn = (I & 1) ? -1.f : 1.f;
             // x_bar of box pixel j: conj(z) in buf, x[2m] = Re z, x[2m+1] = Im z = -buf.y
             auto xbar = [&](int j) {
@@ -789,7 +789,7 @@ __global__ void write_grad_params_kernel(int B, int pstride, const double* __res
 // transposed layout zt[b][k][row] is written, and read back by the adjoint,
 // in contiguous runs of F rows.
 // ---------------------------------------------------------------------------
-template <int E, int MAXT>
+template <int E, int MAXT, int LG>
 __global__ void __launch_bounds__(MAXT) rows_image_batch_kernel(Geo g, int F, const float* __restrict__ images,
                                                                 const float2* __restrict__ tw,
                                                                 const float2* __restrict__ stw,
@@ -808,7 +808,7 @@ __global__ void __launch_bounds__(MAXT) rows_image_batch_kernel(Geo g, int F, co
         __syncthreads();  // buf free
         for (int mm = threadIdx.x; mm < g.M; mm += blockDim.x) buf[sp(mm)] = __ldg(&row[mm]);
         __syncthreads();
-        block_fft<float, E>(buf, g.M, ilog2(g.M), stw);
+        block_fft_sel<float, E, LG>(buf, g.M, stw);
         const float sgn = (i & 1) ? -1.f : 1.f;  // the image fftshift, folded into the rows
         for (int k = threadIdx.x; k < g.K; k += blockDim.x) {
             const float2 x = real_split<float>(buf, g.M, k, tw);
@@ -826,7 +826,7 @@ __global__ void __launch_bounds__(MAXT) rows_image_batch_kernel(Geo g, int F, co
 }
 
 // adjoint of rows_image_batch_kernel: dchi2/d(pixel) of every image row
-template <int E, int MAXT>
+template <int E, int MAXT, int LG>
 __global__ void __launch_bounds__(MAXT) rowsT_image_batch_kernel(Geo g, int F, const float2* __restrict__ stw,
                                                                  const float2* __restrict__ twc,
                                                                  const float2* __restrict__ zbar,
@@ -867,7 +867,7 @@ __global__ void __launch_bounds__(MAXT) rowsT_image_batch_kernel(Geo g, int F, c
             buf[sp(k)] = make_float2(Ep.x - Op.y, -(Ep.y + Op.x));  // conjugated: inverse FFT by a forward one
         }
         __syncthreads();
-        block_fft<float, E>(buf, M, ilog2(M), stw);
+        block_fft_sel<float, E, LG>(buf, M, stw);
         const float sgn = (i & 1) ? -1.f : 1.f;
         float2* grow = reinterpret_cast<float2*>(gimg + ((size_t)b * g.N + i) * g.N);
         for (int mm = threadIdx.x; mm < M; mm += blockDim.x) {
@@ -1178,18 +1178,37 @@ __global__ void iota_kernel(int* __restrict__ idx, int n) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) idx[i] = i;
 }
 
-// (values per thread EE, block-size bound TT) for an FFT with `threads` threads
+// (values per thread EE, block-size bound TT, compile-time log2 length LG)
+// for an FFT of length L_ with E_ values per thread: lengths 2^9..2^13 get the
+// compile-time FFT, others the run-time one (LG = 0)
 #define GBB_CASE_T(E_V, THR, ...)                                                          \
     {                                                                                      \
         constexpr int EE = E_V;                                                            \
+        constexpr int LG = 0;                                                              \
         if ((THR) <= 256) { constexpr int TT = 256; __VA_ARGS__; }                         \
         else if ((THR) <= 512) { constexpr int TT = 512; __VA_ARGS__; }                    \
         else { constexpr int TT = 1024; __VA_ARGS__; }                                     \
     }
-#define GBB_DISPATCH_E(E_, THR, ...)                                      \
+#define GBB_CASE_LG(E_V, LG_V, ...)                                                        \
+    {                                                                                      \
+        constexpr int EE = E_V;                                                            \
+        constexpr int LG = LG_V;                                                           \
+        constexpr int TT = ((1 << LG_V) / E_V) <= 256 ? 256 : ((1 << LG_V) / E_V);          \
+        __VA_ARGS__;                                                                       \
+    }
+#define GBB_CASE_EL(E_V, L_, ...)                                                          \
+    switch (L_) {                                                                          \
+        case 512: GBB_CASE_LG(E_V, 9, __VA_ARGS__) break;                                  \
+        case 1024: GBB_CASE_LG(E_V, 10, __VA_ARGS__) break;                                \
+        case 2048: GBB_CASE_LG(E_V, 11, __VA_ARGS__) break;                                \
+        case 4096: GBB_CASE_LG(E_V, 12, __VA_ARGS__) break;                                \
+        case 8192: GBB_CASE_LG(E_V, 13, __VA_ARGS__) break;                                \
+        default: GBB_CASE_T(E_V, (L_) / (E_V), __VA_ARGS__) break;                         \
+    }
+#define GBB_DISPATCH_E(E_, L_, ...)                                       \
     switch (E_) {                                                         \
-        case 8: GBB_CASE_T(8, THR, __VA_ARGS__) break;                    \
-        case 16: GBB_CASE_T(16, THR, __VA_ARGS__) break;                  \
+        case 8: GBB_CASE_EL(8, L_, __VA_ARGS__) break;                    \
+        case 16: GBB_CASE_EL(16, L_, __VA_ARGS__) break;                  \
         default: throw Err{GALARIO_EINVAL, "unsupported FFT length"};     \
     }
 
@@ -1506,9 +1525,9 @@ static void batch_run(const BatchCall& call) {
             if (image) {
                 const size_t sm = sizeof(float2) * (fft_slots(g.M) + (size_t)g.K * (Fimg + 1));
                 check_smem(sm);
-                GBB_DISPATCH_E(E, fft_threads(g.M, E), {
-                    BCK((cudaError_t)smem_attr((const void*)rows_image_batch_kernel<EE, TT>, sm));
-                    rows_image_batch_kernel<EE, TT><<<dim3((g.N + Fimg - 1) / Fimg, B), fft_threads(g.M, EE), sm, s>>>(
+                GBB_DISPATCH_E(E, g.M, {
+                    BCK((cudaError_t)smem_attr((const void*)rows_image_batch_kernel<EE, TT, LG>, sm));
+                    rows_image_batch_kernel<EE, TT, LG><<<dim3((g.N + Fimg - 1) / Fimg, B), fft_threads(g.M, EE), sm, s>>>(
                         g, Fimg, intensity, tws.first, ws.stage_tw(g.M, EE), zt);
                 });
                 BCK(cudaGetLastError());
@@ -1517,18 +1536,18 @@ static void batch_run(const BatchCall& call) {
             const size_t sm = sizeof(float2) * (fft_slots(g.M) + (size_t)g.K * (2 * Frows + 1)) +
                               sizeof(float) * (g.rmax + 1);
             check_smem(sm);
-            GBB_DISPATCH_E(E, fft_threads(g.M, E), {
-                BCK((cudaError_t)smem_attr((const void*)rows_batch_kernel<EE, TT>, sm));
-                rows_batch_kernel<EE, TT><<<dim3((g.rmax + Frows) / Frows, B), fft_threads(g.M, EE), sm, s>>>(
+            GBB_DISPATCH_E(E, g.M, {
+                BCK((cudaError_t)smem_attr((const void*)rows_batch_kernel<EE, TT, LG>, sm));
+                rows_batch_kernel<EE, TT, LG><<<dim3((g.rmax + Frows) / Frows, B), fft_threads(g.M, EE), sm, s>>>(
                     g, Frows, intensity, mc, tws.first, ws.stage_tw(g.M, EE), zt);
             });
             BCK(cudaGetLastError());
         };
         auto cols = [&](int E) {
             const size_t sm = sizeof(float2) * fft_slots(g.N);
-            GBB_DISPATCH_E(E, fft_threads(g.N, E), {
-                BCK((cudaError_t)smem_attr((const void*)cols_batch_kernel<EE, TT>, sm));
-                cols_batch_kernel<EE, TT><<<dim3(g.K, B), fft_threads(g.N, EE), sm, s>>>(
+            GBB_DISPATCH_E(E, g.N, {
+                BCK((cudaError_t)smem_attr((const void*)cols_batch_kernel<EE, TT, LG>, sm));
+                cols_batch_kernel<EE, TT, LG><<<dim3(g.K, B), fft_threads(g.N, EE), sm, s>>>(
                     g, zt, ws.stage_tw(g.N, EE), win, amp);
             });
             BCK(cudaGetLastError());
@@ -1556,9 +1575,9 @@ static void batch_run(const BatchCall& call) {
         };
         auto colsT = [&](int E) {
             const size_t sm = sizeof(float2) * fft_slots(g.N);
-            GBB_DISPATCH_E(E, fft_threads(g.N, E), {
-                BCK((cudaError_t)smem_attr((const void*)colsT_batch_kernel<EE, TT>, sm));
-                colsT_batch_kernel<EE, TT><<<dim3(g.K, B), fft_threads(g.N, EE), sm, s>>>(
+            GBB_DISPATCH_E(E, g.N, {
+                BCK((cudaError_t)smem_attr((const void*)colsT_batch_kernel<EE, TT, LG>, sm));
+                colsT_batch_kernel<EE, TT, LG><<<dim3(g.K, B), fft_threads(g.N, EE), sm, s>>>(
                     g, gwin, ws.stage_tw(g.N, EE), zbar);
             });
             BCK(cudaGetLastError());
@@ -1567,9 +1586,9 @@ static void batch_run(const BatchCall& call) {
             if (image) {
                 const size_t smi = sizeof(float2) * (fft_slots(g.M) + (size_t)g.K * (Fimg + 1));
                 check_smem(smi);
-                GBB_DISPATCH_E(E, fft_threads(g.M, E), {
-                    BCK((cudaError_t)smem_attr((const void*)rowsT_image_batch_kernel<EE, TT>, smi));
-                    rowsT_image_batch_kernel<EE, TT><<<dim3((g.N + Fimg - 1) / Fimg, B), fft_threads(g.M, EE), smi, s>>>(
+                GBB_DISPATCH_E(E, g.M, {
+                    BCK((cudaError_t)smem_attr((const void*)rowsT_image_batch_kernel<EE, TT, LG>, smi));
+                    rowsT_image_batch_kernel<EE, TT, LG><<<dim3((g.N + Fimg - 1) / Fimg, B), fft_threads(g.M, EE), smi, s>>>(
                         g, Fimg, ws.stage_tw(g.M, EE), tws.second, zbar, grad_intensity);
                 });
                 BCK(cudaGetLastError());
@@ -1578,9 +1597,9 @@ static void batch_run(const BatchCall& call) {
             const size_t sm = sizeof(float2) * (fft_slots(g.M) + (size_t)g.K * (2 * Frows + 1)) +
                               sizeof(float) * (nr + g.rmax + 1);
             check_smem(sm);
-            GBB_DISPATCH_E(E, fft_threads(g.M, E), {
-                BCK((cudaError_t)smem_attr((const void*)rowsT_batch_kernel<EE, TT>, sm));
-                rowsT_batch_kernel<EE, TT><<<dim3((g.rmax + Frows * GrowsT) / (Frows * GrowsT), B), fft_threads(g.M, EE), sm, s>>>(
+            GBB_DISPATCH_E(E, g.M, {
+                BCK((cudaError_t)smem_attr((const void*)rowsT_batch_kernel<EE, TT, LG>, sm));
+                rowsT_batch_kernel<EE, TT, LG><<<dim3((g.rmax + Frows * GrowsT) / (Frows * GrowsT), B), fft_threads(g.M, EE), sm, s>>>(
                     g, Frows, GrowsT, intensity, mc, ws.stage_tw(g.M, EE), tws.second, zbar, grad_intensity, ginc_d, gcentral);
             });
             BCK(cudaGetLastError());

@@ -212,6 +212,61 @@ __device__ void block_fft(C2<T>* buf, int M, int log2M, const C2<T>* __restrict_
     }
 }
 
+// The same FFT with the length a compile-time constant: every stride, mask
+// and thread count below is a constant, so the padded shared-memory offsets
+// of a butterfly's R values fold into immediates (a stride that is a multiple
+// of 16 moves sp() by a constant) instead of being recomputed per value.
+// blockDim.x must be M / E.
+template <typename T, int E, int R, int M, int NS>
+__device__ __forceinline__ void stockham_stage_ct(C2<T>* buf, const C2<T>* __restrict__ stw) {
+    using CT = C2<T>;
+    constexpr int B = E / R, NT = M / E, STRIDE = M / R;
+    const int tid = threadIdx.x;
+    CT v[E];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const int j = tid + b * NT;
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[b * R + r] = buf[sp(j + r * STRIDE)];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        const int j = tid + b * NT;
+        const int k = j & (NS - 1);
+        if constexpr (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[b * R + r] = cmul(v[b * R + r], __ldg(&stw[(r - 1) * NS + k]));
+        }
+        Dft<T, R>::run(&v[b * R]);
+        const int d = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) buf[sp(d + r * NS)] = v[b * R + r];
+    }
+    __syncthreads();
+}
+
+template <typename T, int E, int M, int NS, int BITS>
+__device__ __forceinline__ void block_fft_ct_rec(C2<T>* buf, const C2<T>* __restrict__ stw) {
+    if constexpr (BITS > 0) {
+        constexpr int R = (E >= 16 && BITS >= 4) ? 16 : (E >= 8 && BITS >= 3) ? 8 : (E >= 4 && BITS >= 2) ? 4 : 2;
+        constexpr int RB = R == 16 ? 4 : R == 8 ? 3 : R == 4 ? 2 : 1;
+        stockham_stage_ct<T, E, R, M, NS>(buf, stw);
+        block_fft_ct_rec<T, E, M, NS * R, BITS - RB>(buf, stw + (R - 1) * NS);
+    }
+}
+
+// LG > 0: the compile-time FFT of length 2^LG (L must equal it); LG == 0:
+// the run-time one
+template <typename T, int E, int LG>
+__device__ __forceinline__ void block_fft_sel(C2<T>* buf, int L, const C2<T>* __restrict__ stw) {
+    if constexpr (LG > 0) {
+        block_fft_ct_rec<T, E, (1 << LG), 1, LG>(buf, stw);
+    } else {
+        block_fft<T, E>(buf, L, 31 - __clz(L), stw);
+    }
+}
+
 // Stage twiddles of a length-L FFT with E values per thread (host side):
 // for each stage (radix R, span Ns), W^(r k) for r in [1, R), k in [0, Ns),
 // evaluated in long double.
