@@ -630,7 +630,7 @@ __global__ void __launch_bounds__(MAXT) colsT_batch_kernel(Geo g, const float2* 
 // complex FFT (Hermitian weights), then the sweep adjoint into the profile
 // and the inclination.
 template <int E, int MAXT, int LG>
-__global__ void __launch_bounds__(MAXT) rowsT_batch_kernel(Geo g, int F, int G, const float* __restrict__ intensity,
+__global__ void __launch_bounds__(MAXT, (MAXT <= 256 ? 3 : 1)) rowsT_batch_kernel(Geo g, int F, int G, const float* __restrict__ intensity,
                                                            const ModelConst* __restrict__ mc,
                                                            const float2* __restrict__ stw,
                                                            const float2* __restrict__ twc,
