@@ -377,9 +377,44 @@ __device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, co
 // Accumulators per model and block: chi2, dPA, dRA, dDec
 constexpr int kAcc = 4;
 
+// PTS consecutive entries of a float array, one vector load when aligned and in range
+template <int PTS>
+__device__ __forceinline__ void load_pts(const float* __restrict__ a, long long i0, long long n, float* out) {
+    if (i0 + PTS <= n) {
+        if constexpr (PTS == 4) {
+            const float4 x = __ldg(reinterpret_cast<const float4*>(a + i0));
+            out[0] = x.x; out[1] = x.y; out[2] = x.z; out[3] = x.w;
+            return;
+        } else if constexpr (PTS == 2) {
+            const float2 x = __ldg(reinterpret_cast<const float2*>(a + i0));
+            out[0] = x.x; out[1] = x.y;
+            return;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < PTS; ++j) out[j] = (i0 + j < n) ? __ldg(&a[i0 + j]) : 0.f;
+}
+
+// one 12-float cell gradient record added to the model's cell (three 16-byte atomics)
+__device__ __forceinline__ void emit_cell(float* __restrict__ cg, int cell, const float* r) {
+    float4* dst = reinterpret_cast<float4*>(cg + (size_t)cell * kGRec);
+    atomicAdd(dst, make_float4(r[0], r[1], r[2], r[3]));
+    atomicAdd(dst + 1, make_float4(r[4], r[5], r[6], r[7]));
+    atomicAdd(dst + 2, make_float4(r[8], r[9], r[10], r[11]));
+}
+
 // Grid: x = blocks of kVisThreads * PTS visibilities, y = groups of Bg
 // models.  The hardware issues the x blocks of one group before the next, so
 // the cell records of about Bg models are live in L2 at a time.
+//
+// Thread t of a block owns the PTS consecutive visibilities t*PTS .. t*PTS+PTS-1
+// of the block's span (vector loads; consecutive in the Morton order, so they
+// often share a uv cell).  With the gradient, each thread first sums the cell
+// records of its own runs of equal cells in registers; runs that begin and
+// end inside the thread are added to the cell gradient directly; the thread's
+// first run, when it continues the previous lane's last run, is handed to that
+// lane; the last runs then go through one warp-segmented reduction (shuffles)
+// and one lane per run of equal cells adds it.
 template <bool GRAD, int PTS>
 __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, int Bg, int nd, const float* __restrict__ u,
                                                                 const float* __restrict__ v,
@@ -400,17 +435,12 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
     for (int i = threadIdx.x; i < nb; i += blockDim.x) smc[i] = mc[b0 + i];
     // this thread's points
     float pu[PTS], pv[PTS], pre[PTS], pim[PTS], pw[PTS];
-    const long long base = (long long)blockIdx.x * kVisThreads * PTS + threadIdx.x;
-#pragma unroll
-    for (int j = 0; j < PTS; ++j) {
-        const long long i = base + (long long)j * kVisThreads;
-        const bool in = i < nd;
-        pu[j] = in ? __ldg(&u[i]) : 0.f;
-        pv[j] = in ? __ldg(&v[i]) : 0.f;
-        pre[j] = in ? __ldg(&re[i]) : 0.f;
-        pim[j] = in ? __ldg(&im[i]) : 0.f;
-        pw[j] = in ? __ldg(&w[i]) : 0.f;  // w = 0 marks the padding points
-    }
+    const long long i0 = ((long long)blockIdx.x * kVisThreads + threadIdx.x) * PTS;
+    load_pts<PTS>(u, i0, nd, pu);
+    load_pts<PTS>(v, i0, nd, pv);
+    load_pts<PTS>(re, i0, nd, pre);
+    load_pts<PTS>(im, i0, nd, pim);
+    load_pts<PTS>(w, i0, nd, pw);  // w = 0 marks the padding points
     __syncthreads();
     const long long ncell = (long long)g.K * g.W;
     unsigned err = 0u;
@@ -419,7 +449,15 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
         const int b = b0 + bl;
         const ModelConst m = smc[bl];
         const float* qb = quads + (size_t)b * ncell * kRec;
+        float* cg = cgrad + (size_t)b * ncell * kGRec;
         float acc[kAcc] = {0.f, 0.f, 0.f, 0.f};
+        float run[12], first[12];  // the open run of equal cells; the thread's first run
+        int cur = -1, fcell = -1;
+#pragma unroll
+        for (int cc = 0; cc < 12; ++cc) {
+            run[cc] = 0.f;
+            first[cc] = 0.f;
+        }
 #pragma unroll
         for (int j = 0; j < PTS; ++j) {
             const bool live = pw[j] != 0.f;  // w = 0: padding (or a zero-weight visibility)
@@ -432,77 +470,96 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
             }
             const float dr = p.V.x - pre[j], di = p.V.y - pim[j];
             if (live) acc[0] += pw[j] * (dr * dr + di * di);
-            if (GRAD) {
+            if (GRAD && live) {
                 float rec[12];
-                const bool has = live && p.cell >= 0;
-                if (has) {
-                    // dchi2/dV
-                    const float gx = 2.f * pw[j] * dr, gy = 2.f * pw[j] * di;
-                    // phase shift V = U P: dchi2/dphi = -Im(conj(G) V); phi = 2 pi (u dRA + v dDec)
-                    const float dphi = -(gx * p.V.y - gy * p.V.x);
-                    acc[2] += dphi * 6.28318530717958647692f * pu[j];
-                    acc[3] += dphi * 6.28318530717958647692f * pv[j];
-                    // G_U = G conj(P)
-                    const float gux = gx * p.pc + gy * p.ps, guy = -gx * p.ps + gy * p.pc;
-                    // U = A * (zr, su zi) / |z|
-                    const float ex = p.zr * p.rn, ey = p.zi * p.rn;  // e = z/|z|
-                    const float gA = gux * ex + guy * (p.su * ey);
-                    // gradient w.r.t. e (undo the conjugation for u < 0)
-                    const float gex = p.A * gux, gey = p.su * p.A * guy;
-                    const float dot = ex * gex + ey * gey;
-                    const float gzx = (gex - ex * dot) * p.rn, gzy = (gey - ey * dot) * p.rn;
-                    const float t = p.t, q = p.q;
-                    const float wgt[4] = {(1.f - t) * (1.f - q), t * (1.f - q), t * q, (1.f - t) * q};
+                // dchi2/dV
+                const float gx = 2.f * pw[j] * dr, gy = 2.f * pw[j] * di;
+                // phase shift V = U P: dchi2/dphi = -Im(conj(G) V); phi = 2 pi (u dRA + v dDec)
+                const float dphi = -(gx * p.V.y - gy * p.V.x);
+                acc[2] += dphi * 6.28318530717958647692f * pu[j];
+                acc[3] += dphi * 6.28318530717958647692f * pv[j];
+                // G_U = G conj(P)
+                const float gux = gx * p.pc + gy * p.ps, guy = -gx * p.ps + gy * p.pc;
+                // U = A * (zr, su zi) / |z|
+                const float ex = p.zr * p.rn, ey = p.zi * p.rn;  // e = z/|z|
+                const float gA = gux * ex + guy * (p.su * ey);
+                // gradient w.r.t. e (undo the conjugation for u < 0)
+                const float gex = p.A * gux, gey = p.su * p.A * guy;
+                const float dot = ex * gex + ey * gey;
+                const float gzx = (gex - ex * dot) * p.rn, gzy = (gey - ey * dot) * p.rn;
+                const float t = p.t, q = p.q;
+                const float wgt[4] = {(1.f - t) * (1.f - q), t * (1.f - q), t * q, (1.f - t) * q};
 #pragma unroll
-                    for (int cc = 0; cc < 4; ++cc) {
-                        rec[2 * cc] = wgt[cc] * gzx;
-                        rec[2 * cc + 1] = wgt[cc] * gzy;
-                        rec[8 + cc] = wgt[cc] * gA;
-                    }
-                    // position: q = |a|, t = N/2 + vo su c with a = u'/duv, c = v'/duv;
-                    // da/dPA = -c, dc/dPA = a
-                    const float dzqx = (p.y[3].x - p.y[0].x) + t * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
-                    const float dzqy = (p.y[3].y - p.y[0].y) + t * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
-                    const float dztx = (p.y[1].x - p.y[0].x) + q * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
-                    const float dzty = (p.y[1].y - p.y[0].y) + q * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
-                    const float dAq = (p.am[3] - p.am[0]) + t * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
-                    const float dAt = (p.am[1] - p.am[0]) + q * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
-                    const float gq = gzx * dzqx + gzy * dzqy + gA * dAq;
-                    const float gt = gzx * dztx + gzy * dzty + gA * dAt;
-                    acc[1] += gq * (p.su * (-p.vr)) + gt * (g.vo * p.su * p.ur);
-                } else {
-#pragma unroll
-                    for (int cc = 0; cc < 12; ++cc) rec[cc] = 0.f;
+                for (int cc = 0; cc < 4; ++cc) {
+                    rec[2 * cc] = wgt[cc] * gzx;
+                    rec[2 * cc + 1] = wgt[cc] * gzy;
+                    rec[8 + cc] = wgt[cc] * gA;
                 }
-                // Scatter into the cell record.  Lanes of a warp hold consecutive
-                // visibilities of the spatially sorted dataset, so near the uv
-                // centre many of them hit the same cell: runs of equal cells are
-                // reduced with shuffles first and one lane per run adds atomically.
-                const int key = has ? p.cell : -1 - lane;
-                const int prev = __shfl_up_sync(0xffffffffu, key, 1);
-                const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || key != prev);
-                if (heads != 0xffffffffu) {
-                    const int seg = __popc(heads & ((2u << lane) - 1u));
-                    // only as many halving steps as the longest run needs
-                    const unsigned later = heads & ~((2u << lane) - 1u);
-                    const int run = ((heads >> lane) & 1u) ? (later ? __ffs(later) - 1 : 32) - lane : 0;
-                    const int maxrun = __reduce_max_sync(0xffffffffu, run);
-                    for (int d = 1; d < maxrun; d <<= 1) {
-                        const int seg_d = __shfl_down_sync(0xffffffffu, seg, d);
+                // position: q = |a|, t = N/2 + vo su c with a = u'/duv, c = v'/duv;
+                // da/dPA = -c, dc/dPA = a
+                const float dzqx = (p.y[3].x - p.y[0].x) + t * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
+                const float dzqy = (p.y[3].y - p.y[0].y) + t * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
+                const float dztx = (p.y[1].x - p.y[0].x) + q * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
+                const float dzty = (p.y[1].y - p.y[0].y) + q * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
+                const float dAq = (p.am[3] - p.am[0]) + t * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
+                const float dAt = (p.am[1] - p.am[0]) + q * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
+                const float gq = gzx * dzqx + gzy * dzqy + gA * dAq;
+                const float gt = gzx * dztx + gzy * dzty + gA * dAt;
+                acc[1] += gq * (p.su * (-p.vr)) + gt * (g.vo * p.su * p.ur);
+                // runs of equal cells within the thread, summed in registers
+                if (p.cell == cur) {
 #pragma unroll
-                        for (int cc = 0; cc < 12; ++cc) {
-                            const float o = __shfl_down_sync(0xffffffffu, rec[cc], d);
-                            if (lane + d < 32 && seg_d == seg) rec[cc] += o;
+                    for (int cc = 0; cc < 12; ++cc) run[cc] += rec[cc];
+                } else {
+                    if (cur >= 0) {
+                        if (fcell < 0) {
+                            fcell = cur;
+#pragma unroll
+                            for (int cc = 0; cc < 12; ++cc) first[cc] = run[cc];
+                        } else {
+                            emit_cell(cg, cur, run);  // begins and ends inside this thread
                         }
                     }
-                }
-                if (has && ((heads >> lane) & 1u)) {
-                    float4* dst = reinterpret_cast<float4*>(cgrad + ((size_t)b * ncell + p.cell) * kGRec);
-                    atomicAdd(dst, make_float4(rec[0], rec[1], rec[2], rec[3]));
-                    atomicAdd(dst + 1, make_float4(rec[4], rec[5], rec[6], rec[7]));
-                    atomicAdd(dst + 2, make_float4(rec[8], rec[9], rec[10], rec[11]));
+                    cur = p.cell;
+#pragma unroll
+                    for (int cc = 0; cc < 12; ++cc) run[cc] = rec[cc];
                 }
             }
+        }
+        if (GRAD) {
+            const unsigned full = 0xffffffffu;
+            const int klast = cur >= 0 ? cur : -1 - lane;  // empty lanes get keys no cell matches
+            const int kprev = __shfl_up_sync(full, klast, 1);
+            // the first run continues the previous lane's last run: hand it over
+            const bool pass = fcell >= 0 && lane > 0 && fcell == kprev;
+            if (__ballot_sync(full, pass)) {
+                const bool take = __shfl_down_sync(full, (int)pass, 1) && lane < 31;
+#pragma unroll
+                for (int cc = 0; cc < 12; ++cc) {
+                    const float o = __shfl_down_sync(full, first[cc], 1);
+                    if (take) run[cc] += o;
+                }
+            }
+            if (fcell >= 0 && !pass) emit_cell(cg, fcell, first);
+            // last runs: lanes with equal keys are consecutive; reduce each
+            // segment with shuffles, then its first lane adds it
+            const unsigned heads = __ballot_sync(full, lane == 0 || klast != kprev);
+            if (heads != full) {
+                const int seg = __popc(heads & ((2u << lane) - 1u));
+                // only as many halving steps as the longest segment needs
+                const unsigned later = heads & ~((2u << lane) - 1u);
+                const int len = ((heads >> lane) & 1u) ? (later ? __ffs(later) - 1 : 32) - lane : 0;
+                const int maxlen = __reduce_max_sync(full, len);
+                for (int d = 1; d < maxlen; d <<= 1) {
+                    const int seg_d = __shfl_down_sync(full, seg, d);
+#pragma unroll
+                    for (int cc = 0; cc < 12; ++cc) {
+                        const float o = __shfl_down_sync(full, run[cc], d);
+                        if (lane + d < 32 && seg_d == seg) run[cc] += o;
+                    }
+                }
+            }
+            if (cur >= 0 && ((heads >> lane) & 1u)) emit_cell(cg, cur, run);
         }
         // warp sums of this model's accumulators
 #pragma unroll
@@ -929,23 +986,28 @@ struct Tuner {
         cudaEventDestroy(a);
         cudaEventDestroy(b);
     }
+    // every candidate: one warm-up launch, then the fastest of three timed
+    // launches, the candidates interleaved so that clock or cache drift
+    // between them does not decide
     template <class F> int best(const std::vector<int>& cand, F&& run) {
-        int best_c = cand.empty() ? 8 : cand[0];
-        float best_ms = 1e30f;
-        for (int c : cand) {
-            run(c);  // warm-up
-            cudaEventRecord(a, s);
-            run(c);
-            cudaEventRecord(b, s);
-            if (cudaEventSynchronize(b) != cudaSuccess) break;
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, a, b);
-            if (ms < best_ms) {
-                best_ms = ms;
-                best_c = c;
+        if (cand.empty()) return 8;
+        std::vector<float> best_ms(cand.size(), 1e30f);
+        for (int c : cand) run(c);
+        for (int rep = 0; rep < 3; ++rep) {
+            for (size_t i = 0; i < cand.size(); ++i) {
+                cudaEventRecord(a, s);
+                run(cand[i]);
+                cudaEventRecord(b, s);
+                if (cudaEventSynchronize(b) != cudaSuccess) return cand[0];
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, a, b);
+                best_ms[i] = std::min(best_ms[i], ms);
             }
         }
-        return best_c;
+        size_t k = 0;
+        for (size_t i = 1; i < cand.size(); ++i)
+            if (best_ms[i] < best_ms[k]) k = i;
+        return cand[k];
     }
 };
 
