@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -112,6 +113,10 @@ struct Ctx {
     int device = 0;
     std::mutex mu;
     cudaStream_t stream = nullptr;
+    // second stream: the host-pointer chi2 calls upload the observations
+    // (Re, Im, w) on it while the spectrum passes run on `stream`
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_side_start = nullptr, ev_obs = nullptr;
     DevBuf state, partials, img, prof, u, v, re, im, w, vis, zt, win, amp, quad, urot, vrot;
     double2* phase_tab = nullptr;  // table of the FP64 phase shift (PHASE_T + 1 entries)
     std::map<std::pair<int, int>, void*> tw;   // (N, sizeof(T)) -> table
@@ -139,6 +144,9 @@ struct Ctx {
     void init(int dev) {
         device = dev;
         CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ev_side_start, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ev_obs, cudaEventDisableTiming));
         CK(cudaMallocHost(&host_state, sizeof(DevState)));
         // exp(2 pi i (j - T/2) / T), j in [0, T], evaluated in long double
         std::vector<double2> h(PHASE_T + 1);
@@ -308,7 +316,8 @@ template <typename T> struct Pipe {
     static void enqueue(Ctx& c, cudaStream_t s, int N, double duv, const T* img, const T* prof, int nr, double Rmin,
                         double dR, double dxy, double inc, const ProfileGeom* pg, double v_origin, double dRA,
                         double dDec, double PA, int nd, const T* u, const T* v, const T* re, const T* im, const T* w,
-                        CT* vis_out, bool chi2, double* chi2_out, DevState* st, bool have_extent) {
+                        CT* vis_out, bool chi2, double* chi2_out, DevState* st, bool have_extent,
+                        const std::function<void()>& before_vis = std::function<void()>()) {
         const int C = N / 2 + 1;
         const CT* tw = c.twiddles<T>(N);
         CT* zt = as<CT>(c.zt, (size_t)C * N);
@@ -370,9 +379,28 @@ template <typename T> struct Pipe {
         a.partials = chi2 ? partials : nullptr;
         a.chi2_out = chi2_out;
         a.state = st;
+        if (before_vis) before_vis();
         if (nd > 0) timed(c, s, ST_VIS, [&] { CK(L::vis(a, s)); });
     }
 };
+
+// Upload the observations of a host-pointer chi2 call on the side stream,
+// ordered after everything already on `s`; returns the hook that makes `s`
+// wait for them just before the visibility pass, so that the copies overlap
+// the extent, row, column and cell-record passes.
+template <typename T>
+std::function<void()> upload_obs(Ctx& c, cudaStream_t s, T* re_d, const T* re, T* im_d, const T* im, T* w_d,
+                                 const T* w, int nd) {
+    CK(cudaEventRecord(c.ev_side_start, s));
+    CK(cudaStreamWaitEvent(c.side, c.ev_side_start, 0));
+    return [&c, s, re_d, re, im_d, im, w_d, w, nd] {
+        h2d(re_d, re, sizeof(T) * (size_t)nd, c.side);
+        h2d(im_d, im, sizeof(T) * (size_t)nd, c.side);
+        h2d(w_d, w, sizeof(T) * (size_t)nd, c.side);
+        CK(cudaEventRecord(c.ev_obs, c.side));
+        CK(cudaStreamWaitEvent(s, c.ev_obs, 0));
+    };
+}
 
 template <typename T> struct Api {
     using CT = C2<T>;
@@ -425,17 +453,16 @@ template <typename T> struct Api {
         T* im_d = as<T>(c.im, (size_t)nd);
         T* w_d = as<T>(c.w, (size_t)nd);
         DevState* st = as<DevState>(c.state, 1);
+        const auto obs = upload_obs<T>(c, s, re_d, re, im_d, im, w_d, w, nd);
         timed(c, s, ST_H2D, [&] {
             h2d(img_d, img, sizeof(T) * (size_t)N * N, s);
             h2d(u_d, u, sizeof(T) * (size_t)nd, s);
             h2d(v_d, v, sizeof(T) * (size_t)nd, s);
-            h2d(re_d, re, sizeof(T) * (size_t)nd, s);
-            h2d(im_d, im, sizeof(T) * (size_t)nd, s);
-            h2d(w_d, w, sizeof(T) * (size_t)nd, s);
         });
         CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
         Pipe<T>::enqueue(c, s, N, (double)duv, img_d, nullptr, 0, 0, 0, 0, 0, nullptr, (double)v_origin, (double)dRA,
-                         (double)dDec, (double)PA, nd, u_d, v_d, re_d, im_d, w_d, nullptr, true, nullptr, st, false);
+                         (double)dDec, (double)PA, nd, u_d, v_d, re_d, im_d, w_d, nullptr, true, nullptr, st, false,
+                         obs);
         finish(c, st);
         *chi2 = (T)c.host_state->chi2;
     }
@@ -482,17 +509,15 @@ template <typename T> struct Api {
         T* im_d = as<T>(c.im, (size_t)nd);
         T* w_d = as<T>(c.w, (size_t)nd);
         DevState* st = as<DevState>(c.state, 1);
+        const auto obs = upload_obs<T>(c, s, re_d, re, im_d, im, w_d, w, nd);
         timed(c, s, ST_H2D, [&] {
             h2d(I_d, I, sizeof(T) * (size_t)nr, s);
             h2d(u_d, u, sizeof(T) * (size_t)nd, s);
             h2d(v_d, v, sizeof(T) * (size_t)nd, s);
-            h2d(re_d, re, sizeof(T) * (size_t)nd, s);
-            h2d(im_d, im, sizeof(T) * (size_t)nd, s);
-            h2d(w_d, w, sizeof(T) * (size_t)nd, s);
         });
         CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
         Pipe<T>::enqueue(c, s, N, (double)duv, nullptr, I_d, nr, Rmin, dR, dxy, inc, &pg, 1.0, dRA, dDec, PA, nd, u_d,
-                         v_d, re_d, im_d, w_d, nullptr, true, nullptr, st, false);
+                         v_d, re_d, im_d, w_d, nullptr, true, nullptr, st, false, obs);
         finish(c, st);
         *chi2 = (T)c.host_state->chi2;
     }
