@@ -55,6 +55,7 @@ constexpr int kVisWarps = kVisThreads / 32;
 constexpr int kRowsPerCta = 16;  // folded image rows (up to two box rows each) per CTA in the row adjoint
 constexpr int kRec = 12;        // floats per forward cell record: 4 complex corners, 4 moduli (48 B)
 constexpr int kGRec = 12;       // floats per gradient cell record
+constexpr int kTmaCols = 100;   // column-pass shape code: E + kTmaCols selects the TMA-fed variant
 
 struct ModelConst {
     DF cu, sv;            // cos(PA) / duv, sin(PA) / duv: (u, v) -> rotated grid coordinates
@@ -226,6 +227,107 @@ __global__ void __launch_bounds__(MAXT) cols_batch_kernel(Geo g, const float2* _
         if ((r & 1) ^ par) x = make_float2(-x.x, -x.y);
         wcol[q] = x;
         acol[q] = sqrtf(fmaf(x.x, x.x, x.y * x.y));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// TMA-fed column pass: persistent CTAs, each looping over columns
+// c = blockIdx.x, blockIdx.x + gridDim.x, ...; the R non-zero entries of the
+// next column are fetched by a 1D bulk copy (cp.async.bulk, completion counted
+// on an mbarrier) into one of two staging buffers while the current column is
+// transformed.  Requires R*8 bytes to be a multiple of 16 (R even), which also
+// keeps every column start 16-byte aligned.  Waits are bounded: a wait that
+// gives up sets ERR_SPIN, waits (bounded) for the copies it issued and ends
+// the CTA.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst_smem, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst_smem)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// true once the barrier's phase with this parity has completed; false when
+// the bounded number of polls ran out
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    const unsigned a = smem_u32(bar);
+    for (int it = 0; it < (1 << 22); ++it) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <int E, int MAXT, int LG>
+__global__ void __launch_bounds__(MAXT) cols_batch_tma_kernel(Geo g, int total, const float2* __restrict__ zt,
+                                                              const float2* __restrict__ stw,
+                                                              float2* __restrict__ win, float* __restrict__ amp,
+                                                              DevState* st) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* stg = reinterpret_cast<float2*>(smem_raw);  // [2][R], 16-byte aligned
+    float2* buf = stg + 2 * (size_t)g.R;
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(buf + fft_slots(g.N));
+    const unsigned bytes = (unsigned)g.R * 8u;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int c = blockIdx.x;
+    if (threadIdx.x == 0 && c < total) bulk_load(stg, zt + (size_t)c * g.R, bytes, &bar[0]);
+    int issued = (c < total) ? 1 : 0, consumed = 0;
+    for (int i = 0; c < total; ++i, c += gridDim.x) {
+        const int cur = i & 1;
+        const int nxt = c + gridDim.x;
+        if (threadIdx.x == 0 && nxt < total) {
+            // the other buffer was read by all threads before the barriers of the previous column
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            bulk_load(stg + (size_t)(cur ^ 1) * g.R, zt + (size_t)nxt * g.R, bytes, &bar[cur ^ 1]);
+            ++issued;
+        }
+        const bool ok = mbar_wait(&bar[cur], (unsigned)((i >> 1) & 1));
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0) {
+                atomicOr(&st->err, ERR_SPIN);
+                for (int j = consumed; j < issued; ++j) (void)mbar_wait(&bar[j & 1], (unsigned)((j >> 1) & 1));
+            }
+            __syncthreads();
+            return;
+        }
+        ++consumed;
+        const float2* col = stg + (size_t)cur * g.R;
+        for (int r = threadIdx.x; r < g.N; r += blockDim.x) {
+            const int q = r - g.band0;
+            buf[sp(r)] = (q >= 0 && q < g.R) ? col[q] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        block_fft_sel<float, E, LG>(buf, g.N, stw);
+        const int b = c / g.K, k = c - b * g.K;
+        const int par = (k + g.N / 2) & 1;
+        float2* wcol = win + ((size_t)b * g.K + k) * g.W;
+        float* acol = amp + ((size_t)b * g.K + k) * g.W;
+        for (int q = threadIdx.x; q < g.W; q += blockDim.x) {
+            const int r = g.r0 + q;
+            float2 x = buf[sp(r)];
+            if ((r & 1) ^ par) x = make_float2(-x.x, -x.y);
+            wcol[q] = x;
+            acol[q] = sqrtf(fmaf(x.x, x.x, x.y * x.y));
+        }
+        __syncthreads();  // buf and this staging buffer are free again
     }
 }
 
@@ -1605,7 +1707,27 @@ static void batch_run(const BatchCall& call) {
             });
             BCK(cudaGetLastError());
         };
-        auto cols = [&](int E) {
+        // column pass shape: E values per thread, + kTmaCols for the TMA-fed persistent variant
+        const bool tma_ok = (g.R % 2 == 0) &&
+                            sizeof(float2) * (2 * (size_t)g.R + fft_slots(g.N)) + 16 <= 200 * 1024;
+        auto cols = [&](int shape) {
+            const int E = shape % kTmaCols;
+            if (shape >= kTmaCols) {
+                const size_t sm = sizeof(float2) * (2 * (size_t)g.R + fft_slots(g.N)) + 2 * sizeof(unsigned long long);
+                const int total = g.K * B;
+                GBB_DISPATCH_E(E, g.N, {
+                    const void* fn = (const void*)cols_batch_tma_kernel<EE, TT, LG>;
+                    BCK((cudaError_t)smem_attr(fn, sm));
+                    int per_sm = 0;
+                    BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cols_batch_tma_kernel<EE, TT, LG>,
+                                                                      fft_threads(g.N, EE), sm));
+                    const int grid = std::max(1, std::min(total, num_sms() * std::max(per_sm, 1)));
+                    cols_batch_tma_kernel<EE, TT, LG><<<grid, fft_threads(g.N, EE), sm, s>>>(
+                        g, total, zt, ws.stage_tw(g.N, EE), win, amp, st);
+                });
+                BCK(cudaGetLastError());
+                return;
+            }
             const size_t sm = sizeof(float2) * fft_slots(g.N);
             GBB_DISPATCH_E(E, g.N, {
                 BCK((cudaError_t)smem_attr((const void*)cols_batch_kernel<EE, TT, LG>, sm));
@@ -1691,7 +1813,10 @@ static void batch_run(const BatchCall& call) {
             if (grad) zero_grads();
             Tuner tu(s);
             sh.e_rows = tu.best(fft_candidates(g.M), [&](int e) { rows(e); });
-            sh.e_cols = tu.best(fft_candidates(g.N), [&](int e) { cols(e); });
+            std::vector<int> col_shapes = fft_candidates(g.N);
+            if (tma_ok)
+                for (int e : fft_candidates(g.N)) col_shapes.push_back(e + kTmaCols);
+            sh.e_cols = tu.best(col_shapes, [&](int e) { cols(e); });
             sh.pts = tu.best({2, 4}, [&](int p) { vis(p); });
             if (grad) {
                 quadT_batch_kernel<<<num_sms() * 8, 256, 0, s>>>(g, B, cgrad, win, amp, gwin);
