@@ -450,13 +450,31 @@ __device__ __forceinline__ void load_pts(const float* __restrict__ a, long long 
     for (int j = 0; j < PTS; ++j) out[j] = (i0 + j < n) ? __ldg(&a[i0 + j]) : 0.f;
 }
 
-// one 12-float cell gradient record added to the model's cell (three 16-byte atomics)
-__device__ __forceinline__ void emit_cell(float* __restrict__ cg, int cell, const float* r) {
+// A run of visibilities in one cell is summed as the moments of its corner
+// gradients g = (dchi2/dRe z, dchi2/dIm z, dchi2/dA): M = (sum g, sum g t,
+// sum g q, sum g t q), 12 floats [moment][component].  The cell's corner
+// weights are (1-t)(1-q), t(1-q), tq, (1-t)q, so the corner sums follow from
+// the moments; they are added to the model's 12-float cell record
+// (re/im of corners 0..3, then the moduli of corners 0..3) with three 16-byte
+// atomics.
+__device__ __forceinline__ void emit_cell(float* __restrict__ cg, int cell, const float* M) {
+    float r[12];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float m1 = M[i], mt = M[3 + i], mq = M[6 + i], mtq = M[9 + i];
+        const float c[4] = {(m1 - mt) - (mq - mtq), mt - mtq, mtq, mq - mtq};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (i < 2) r[2 * k + i] = c[k];
+            else r[8 + k] = c[k];
+        }
+    }
     float4* dst = reinterpret_cast<float4*>(cg + (size_t)cell * kGRec);
     atomicAdd(dst, make_float4(r[0], r[1], r[2], r[3]));
     atomicAdd(dst + 1, make_float4(r[4], r[5], r[6], r[7]));
     atomicAdd(dst + 2, make_float4(r[8], r[9], r[10], r[11]));
 }
+constexpr int kFirstStride = 13;  // shared-memory slot of a thread's first run (odd: no bank conflicts)
 
 // Grid: x = blocks of kVisThreads * PTS visibilities, y = groups of Bg
 // models.  The hardware issues the x blocks of one group before the next, so
@@ -487,6 +505,9 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
     // per-warp sums [Bg][kAcc][warps]: every slot is written once, no zeroing
     // and no barrier between models
     float* wacc = reinterpret_cast<float*>(smc + Bg);
+    // each thread's first run of equal cells (moments), read by the previous lane
+    float* fst_all = wacc + Bg * kAcc * kVisWarps;
+    float* fst = fst_all + threadIdx.x * kFirstStride;
     for (int i = threadIdx.x; i < nb; i += blockDim.x) smc[i] = mc[b0 + i];
     // this thread's points
     float pu[PTS], pv[PTS], pre[PTS], pim[PTS], pw[PTS];
@@ -506,13 +527,10 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
         const float4* qb = wel + (size_t)b * ncell;
         float* cg = cgrad + (size_t)b * ncell * kGRec;
         float acc[kAcc] = {0.f, 0.f, 0.f, 0.f};
-        float run[12], first[12];  // the open run of equal cells; the thread's first run
+        float run[12];  // moments of the open run of equal cells
         int cur = -1, fcell = -1;
 #pragma unroll
-        for (int cc = 0; cc < 12; ++cc) {
-            run[cc] = 0.f;
-            first[cc] = 0.f;
-        }
+        for (int cc = 0; cc < 12; ++cc) run[cc] = 0.f;
 #pragma unroll
         for (int j = 0; j < PTS; ++j) {
             const bool live = pw[j] != 0.f;  // w = 0: padding (or a zero-weight visibility)
@@ -526,7 +544,6 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
             const float dr = p.V.x - pre[j], di = p.V.y - pim[j];
             if (live) acc[0] += pw[j] * (dr * dr + di * di);
             if (GRAD && live) {
-                float rec[12];
                 // dchi2/dV
                 const float gx = 2.f * pw[j] * dr, gy = 2.f * pw[j] * di;
                 // phase shift V = U P: dchi2/dphi = -Im(conj(G) V); phi = 2 pi (u dRA + v dDec)
@@ -543,13 +560,6 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
                 const float dot = ex * gex + ey * gey;
                 const float gzx = (gex - ex * dot) * p.rn, gzy = (gey - ey * dot) * p.rn;
                 const float t = p.t, q = p.q;
-                const float wgt[4] = {(1.f - t) * (1.f - q), t * (1.f - q), t * q, (1.f - t) * q};
-#pragma unroll
-                for (int cc = 0; cc < 4; ++cc) {
-                    rec[2 * cc] = wgt[cc] * gzx;
-                    rec[2 * cc + 1] = wgt[cc] * gzy;
-                    rec[8 + cc] = wgt[cc] * gA;
-                }
                 // position: q = |a|, t = N/2 + vo su c with a = u'/duv, c = v'/duv;
                 // da/dPA = -c, dc/dPA = a
                 const float dzqx = (p.y[3].x - p.y[0].x) + t * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
@@ -561,23 +571,29 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
                 const float gq = gzx * dzqx + gzy * dzqy + gA * dAq;
                 const float gt = gzx * dztx + gzy * dzty + gA * dAt;
                 acc[1] += gq * (p.su * (-p.vr)) + gt * (g.vo * p.su * p.ur);
-                // runs of equal cells within the thread, summed in registers
+                // runs of equal cells within the thread, summed as moments in registers
+                const float gv[3] = {gzx, gzy, gA};
+                const float mom[4] = {1.f, t, q, t * q};
                 if (p.cell == cur) {
 #pragma unroll
-                    for (int cc = 0; cc < 12; ++cc) run[cc] += rec[cc];
+                    for (int mm = 0; mm < 4; ++mm)
+#pragma unroll
+                        for (int i = 0; i < 3; ++i) run[3 * mm + i] = fmaf(gv[i], mom[mm], run[3 * mm + i]);
                 } else {
                     if (cur >= 0) {
                         if (fcell < 0) {
                             fcell = cur;
 #pragma unroll
-                            for (int cc = 0; cc < 12; ++cc) first[cc] = run[cc];
+                            for (int cc = 0; cc < 12; ++cc) fst[cc] = run[cc];
                         } else {
                             emit_cell(cg, cur, run);  // begins and ends inside this thread
                         }
                     }
                     cur = p.cell;
 #pragma unroll
-                    for (int cc = 0; cc < 12; ++cc) run[cc] = rec[cc];
+                    for (int mm = 0; mm < 4; ++mm)
+#pragma unroll
+                        for (int i = 0; i < 3; ++i) run[3 * mm + i] = gv[i] * mom[mm];
                 }
             }
         }
@@ -587,15 +603,14 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
             const int kprev = __shfl_up_sync(full, klast, 1);
             // the first run continues the previous lane's last run: hand it over
             const bool pass = fcell >= 0 && lane > 0 && fcell == kprev;
-            if (__ballot_sync(full, pass)) {
-                const bool take = __shfl_down_sync(full, (int)pass, 1) && lane < 31;
+            __syncwarp();
+            const bool take = __shfl_down_sync(full, (int)pass, 1) && lane < 31;
+            if (take) {
+                const float* nf = fst + kFirstStride;  // the next lane's slot
 #pragma unroll
-                for (int cc = 0; cc < 12; ++cc) {
-                    const float o = __shfl_down_sync(full, first[cc], 1);
-                    if (take) run[cc] += o;
-                }
+                for (int cc = 0; cc < 12; ++cc) run[cc] += nf[cc];
             }
-            if (fcell >= 0 && !pass) emit_cell(cg, fcell, first);
+            if (fcell >= 0 && !pass) emit_cell(cg, fcell, fst);
             // last runs: lanes with equal keys are consecutive; reduce each
             // segment with shuffles, then its first lane adds it
             const unsigned heads = __ballot_sync(full, lane == 0 || klast != kprev);
@@ -615,6 +630,7 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
                 }
             }
             if (cur >= 0 && ((heads >> lane) & 1u)) emit_cell(cg, cur, run);
+            __syncwarp();  // the slots are rewritten for the next model
         }
         // warp sums of this model's accumulators
 #pragma unroll
@@ -1682,7 +1698,8 @@ static void batch_run(const BatchCall& call) {
         };
         auto vis = [&](int pts) {
             const int vb = (int)((d->nd_pad + (long long)kVisThreads * pts - 1) / ((long long)kVisThreads * pts));
-            const size_t vsm = sizeof(ModelConst) * Bg + sizeof(float) * Bg * kAcc * kVisWarps;
+            const size_t vsm = sizeof(ModelConst) * Bg + sizeof(float) * Bg * kAcc * kVisWarps +
+                               (grad ? sizeof(float) * kVisThreads * kFirstStride : 0);
             const dim3 grid(vb, ngroups);
 #define GBB_VIS(G_, P_)                                                                                        \
     do {                                                                                                       \
