@@ -812,6 +812,10 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 256 ? 3 : 1)) rowsT_batch_kerne
             __syncthreads();
             // Hermitian weights: Y~0 = Re Y0, Y~k = Yk/2 (0<k<M), Y~M = Re YM; zero for k >= K
             for (int k = threadIdx.x; k < M; k += blockDim.x) {
+                if (k >= g.K && M - k >= g.K) {  // both partners outside the K computed columns
+                    buf[sp(k)] = make_float2(0.f, 0.f);
+                    continue;
+                }
                 auto yk = [&](int kk) -> float2 {
                     if (kk >= g.K) return make_float2(0.f, 0.f);
                     const float2 y = stg[kk * S + slot];
@@ -974,6 +978,10 @@ __global__ void __launch_bounds__(MAXT) rowsT_image_batch_kernel(Geo g, int F, c
         __syncthreads();
         // Hermitian weights: Y~0 = Re Y0, Y~k = Yk/2 (0<k<M), Y~M = Re YM; zero for k >= K
         for (int k = threadIdx.x; k < M; k += blockDim.x) {
+            if (k >= g.K && M - k >= g.K) {  // both partners outside the K computed columns
+                buf[sp(k)] = make_float2(0.f, 0.f);
+                continue;
+            }
             auto yk = [&](int kk) -> float2 {
                 if (kk >= g.K) return make_float2(0.f, 0.f);
                 const float2 y = stg[kk * S + rr];
