@@ -168,30 +168,32 @@ __global__ void __launch_bounds__(MAXT) rows_batch_kernel(Geo g, int F, const fl
         for (int c = threadIdx.x; c <= g.rmax; c += blockDim.x)
             val[c] = sweep_pixel<float>(off + g.rmax - a, off + g.rmax - c, Ib, g.nr, g.Rmin, g.dR, g.inv_dR, g.dxy,
                                         m.inv_cos_inc, g.rmax, off, g.sr_to_px);
-        for (int side = 0; side < 2; ++side) {
-            const int i_box = side ? g.rmax + a : g.rmax - a;
-            if (side && (a == 0 || i_box >= 2 * g.rmax)) break;  // uniform
-            const int I = off + i_box;
-            const int slot = side ? F + (i_box - lo1) : (i_box - lo0);
-            __syncthreads();  // val ready; buf free
-            for (int mm = threadIdx.x; mm < g.M; mm += blockDim.x) {
-                const int j0 = 2 * mm - off, j1 = j0 + 1;
-                float x0 = 0.f, x1 = 0.f;
-                if (j0 >= 0 && j0 < 2 * g.rmax) x0 = val[abs(g.rmax - j0)];
-                if (j1 >= 0 && j1 < 2 * g.rmax) x1 = val[abs(g.rmax - j1)];
-                if (I == g.N / 2) {
-                    if (2 * mm == g.N / 2) x0 = m.central;
-                    if (2 * mm + 1 == g.N / 2) x1 = m.central;
-                }
-                buf[sp(mm)] = make_float2(x0, x1);
+        // the mirror rows rmax - a and rmax + a hold the same pixels and have
+        // the same row-sign parity: one transform serves both
+        const int I = off + g.rmax - a;
+        const int slot0 = (g.rmax - a) - lo0;
+        const bool mirror = a > 0 && a < g.rmax;
+        const int slot1 = mirror ? F + (g.rmax + a - lo1) : -1;
+        __syncthreads();  // val ready; buf free
+        for (int mm = threadIdx.x; mm < g.M; mm += blockDim.x) {
+            const int j0 = 2 * mm - off, j1 = j0 + 1;
+            float x0 = 0.f, x1 = 0.f;
+            if (j0 >= 0 && j0 < 2 * g.rmax) x0 = val[abs(g.rmax - j0)];
+            if (j1 >= 0 && j1 < 2 * g.rmax) x1 = val[abs(g.rmax - j1)];
+            if (I == g.N / 2) {
+                if (2 * mm == g.N / 2) x0 = m.central;
+                if (2 * mm + 1 == g.N / 2) x1 = m.central;
             }
-            __syncthreads();
-            block_fft_sel<float, E, LG>(buf, g.M, stw);
-            const float sgn = (I & 1) ? -1.f : 1.f;
-            for (int k = threadIdx.x; k < g.K; k += blockDim.x) {
-                const float2 x = real_split<float>(buf, g.M, k, tw);
-                stg[k * S + slot] = make_float2(sgn * x.x, sgn * x.y);
-            }
+            buf[sp(mm)] = make_float2(x0, x1);
+        }
+        __syncthreads();
+        block_fft_sel<float, E, LG>(buf, g.M, stw);
+        const float sgn = (I & 1) ? -1.f : 1.f;
+        for (int k = threadIdx.x; k < g.K; k += blockDim.x) {
+            const float2 x = real_split<float>(buf, g.M, k, tw);
+            const float2 y = make_float2(sgn * x.x, sgn * x.y);
+            stg[k * S + slot0] = y;
+            if (mirror) stg[k * S + slot1] = y;
         }
     }
     __syncthreads();
@@ -803,48 +805,50 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 256 ? 3 : 1)) rowsT_batch_kerne
     for (int ff = 0; ff < n0; ++ff) {
         const int a = a0 + ff;  // folded row
         // sum of the pixel adjoints over the (up to) four mirror images
-        // (+-x, +-y) of every folded pixel of this folded row
-        for (int side = 0; side < 2; ++side) {
-            const int i_box = side ? g.rmax + a : g.rmax - a;
-            if (side && (a == 0 || i_box >= 2 * g.rmax)) break;  // uniform
-            const int I = off + i_box;
-            const int slot = side ? F + (i_box - lo1) : (i_box - lo0);
-            __syncthreads();
-            // Hermitian weights: Y~0 = Re Y0, Y~k = Yk/2 (0<k<M), Y~M = Re YM; zero for k >= K
-            for (int k = threadIdx.x; k < M; k += blockDim.x) {
-                if (k >= g.K && M - k >= g.K) {  // both partners outside the K computed columns
-                    buf[sp(k)] = make_float2(0.f, 0.f);
-                    continue;
-                }
-                auto yk = [&](int kk) -> float2 {
-                    if (kk >= g.K) return make_float2(0.f, 0.f);
-                    const float2 y = stg[kk * S + slot];
-                    if (kk == 0 || kk == M) return make_float2(y.x, 0.f);
-                    return make_float2(0.5f * y.x, 0.5f * y.y);
-                };
-                const float2 ya = yk(k), yc = yk(M - k);
-                // E' = a + conj(c), O' = (a - conj(c)) e^{+2 pi i k/N}, Z = E' + i O'
-                const float2 Ep = make_float2(ya.x + yc.x, ya.y - yc.y);
-                const float2 d = make_float2(ya.x - yc.x, ya.y + yc.y);
-                const float2 w = twc[k];  // e^{+2 pi i k / N}
-                const float2 Op = make_float2(d.x * w.x - d.y * w.y, d.x * w.y + d.y * w.x);
-                // Z = E' + i O', stored conjugated: the inverse FFT is conj(FFT(conj(Z)))
-                buf[sp(k)] = make_float2(Ep.x - Op.y, -(Ep.y + Op.x));
+        // (+-x, +-y) of every folded pixel of this folded row.  The mirror
+        // rows rmax - a and rmax + a have the same row sign, so their spectra
+        // are added first and one inverse transform serves both.
+        const int I = off + g.rmax - a;
+        const int slot0 = (g.rmax - a) - lo0;
+        const bool mirror = a > 0 && a < g.rmax;
+        const int slot1 = mirror ? F + (g.rmax + a - lo1) : slot0;
+        const float wm = mirror ? 1.f : 0.f;
+        __syncthreads();
+        // Hermitian weights: Y~0 = Re Y0, Y~k = Yk/2 (0<k<M), Y~M = Re YM; zero for k >= K
+        for (int k = threadIdx.x; k < M; k += blockDim.x) {
+            if (k >= g.K && M - k >= g.K) {  // both partners outside the K computed columns
+                buf[sp(k)] = make_float2(0.f, 0.f);
+                continue;
             }
-            __syncthreads();
-            block_fft_sel<float, E, LG>(buf, M, stw);
-            const float sgn = (I & 1) ? -1.f : 1.f;
-            // x_bar of box pixel j: conj(z) in buf, x[2m] = Re z, x[2m+1] = Im z = -buf.y
-            auto xbar = [&](int j) {
-                const int J = j + off;
-                const float2 zz = buf[sp(J >> 1)];
-                return sgn * ((J & 1) ? -zz.y : zz.x);
+            auto yk = [&](int kk) -> float2 {
+                if (kk >= g.K) return make_float2(0.f, 0.f);
+                const float2 y0 = stg[kk * S + slot0], y1 = stg[kk * S + slot1];
+                const float2 y = make_float2(fmaf(wm, y1.x, y0.x), fmaf(wm, y1.y, y0.y));
+                if (kk == 0 || kk == M) return make_float2(y.x, 0.f);
+                return make_float2(0.5f * y.x, 0.5f * y.y);
             };
-            for (int c = threadIdx.x; c <= g.rmax; c += blockDim.x) {  // each c stays with one thread
-                float acc = xbar(g.rmax - c);
-                if (c > 0 && c < g.rmax) acc += xbar(g.rmax + c);
-                fold[c] = side ? fold[c] + acc : acc;
-            }
+            const float2 ya = yk(k), yc = yk(M - k);
+            // E' = a + conj(c), O' = (a - conj(c)) e^{+2 pi i k/N}, Z = E' + i O'
+            const float2 Ep = make_float2(ya.x + yc.x, ya.y - yc.y);
+            const float2 d = make_float2(ya.x - yc.x, ya.y + yc.y);
+            const float2 w = twc[k];  // e^{+2 pi i k / N}
+            const float2 Op = make_float2(d.x * w.x - d.y * w.y, d.x * w.y + d.y * w.x);
+            // Z = E' + i O', stored conjugated: the inverse FFT is conj(FFT(conj(Z)))
+            buf[sp(k)] = make_float2(Ep.x - Op.y, -(Ep.y + Op.x));
+        }
+        __syncthreads();
+        block_fft_sel<float, E, LG>(buf, M, stw);
+        const float sgn = (I & 1) ? -1.f : 1.f;
+        // x_bar of box pixel j: conj(z) in buf, x[2m] = Re z, x[2m+1] = Im z = -buf.y
+        auto xbar = [&](int j) {
+            const int J = j + off;
+            const float2 zz = buf[sp(J >> 1)];
+            return sgn * ((J & 1) ? -zz.y : zz.x);
+        };
+        for (int c = threadIdx.x; c <= g.rmax; c += blockDim.x) {  // each c stays with one thread
+            float acc = xbar(g.rmax - c);
+            if (c > 0 && c < g.rmax) acc += xbar(g.rmax + c);
+            fold[c] = acc;
         }
         __syncthreads();
         // sweep adjoint of the folded row; (a, c) = (0, 0) is the central pixel alone
