@@ -65,7 +65,13 @@ __global__ void __launch_bounds__(MAXT) rows_profile_kernel(const T* __restrict_
     CT* buf = reinterpret_cast<CT*>(smem_raw);
     const int M = N / 2;
     const int off = N / 2 - rmax;
-    const int I = off + blockIdx.x;  // image row
+    // Block a transforms image row I = N/2 - a.  The swept image depends on
+    // |y| only, so row N/2 + a (0 < a < rmax) holds the same pixels, and its
+    // row sign (-1)^I has the same parity: the result is written to both.
+    const int a_fold = blockIdx.x;
+    const int I = off + rmax - a_fold;
+    const bool mirror = a_fold > 0 && a_fold < rmax;
+    const int I2 = off + rmax + a_fold;
     const T sr_to_px = dxy * dxy;
     for (int m = threadIdx.x; m < M; m += blockDim.x) {
         const int J0 = 2 * m, J1 = 2 * m + 1;
@@ -83,7 +89,9 @@ __global__ void __launch_bounds__(MAXT) rows_profile_kernel(const T* __restrict_
     const T sgn = (I & 1) ? (T)-1 : (T)1;
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
         CT x = real_split<T>(buf, M, k, tw);
-        zt[(size_t)k * N + I] = CT{sgn * x.x, sgn * x.y};
+        const CT y = CT{sgn * x.x, sgn * x.y};
+        zt[(size_t)k * N + I] = y;
+        if (mirror) zt[(size_t)k * N + I2] = y;
     }
 }
 
@@ -667,8 +675,8 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
             auto kern = rows_profile_kernel<T, EE, TT>;
             e = set_smem(kern, c.smem);
             if (e == cudaSuccess) {
-                kern<<<nrows, c.threads, c.smem, s>>>(intensity, nr, (T)Rmin, (T)dR, (T)(1.0 / dR), (T)dxy,
-                                                      inv_cos, rmax, (T)central_value, N, tw, stw, zt, state, duv);
+                kern<<<rmax + 1, c.threads, c.smem, s>>>(intensity, nr, (T)Rmin, (T)dR, (T)(1.0 / dR), (T)dxy,
+                                                         inv_cos, rmax, (T)central_value, N, tw, stw, zt, state, duv);
                 e = cudaGetLastError();
             }
         });
