@@ -341,8 +341,12 @@ template <typename T> struct Pipe {
             });
         }
         // window layout: column k at win + k*N, rows [r0, r0+W) contiguous
-        timed(c, s, ST_COLS,
-              [&] { CK(L::cols(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, -1, -1, -1, st, duv, true, s)); });
+        timed(c, s, ST_COLS, [&] {
+            if (img)
+                CK(L::cols(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, -1, -1, -1, st, duv, true, s));
+            else
+                CK(L::cols_profile(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, st, duv, s));
+        });
         timed(c, s, ST_QUAD, [&] { CK(L::quads(win, amp, 1, N, C, st, quads, qcap, -1, -1, -1, s)); });
         typename L::VisArgs a;
         a.spec = win;

@@ -106,6 +106,11 @@ template <typename T> struct Launch {
     // the device-derived window.
     // amp_out (optional, same layout as out) receives |out|, so the visibility
     // pass gathers amplitudes instead of recomputing 4 moduli per point.
+    // column pass of a swept profile (real, even columns): two columns per
+    // complex transform; device window; output sign applied
+    static cudaError_t cols_profile(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
+                                    T* amp_out, long long s_row, long long s_col, const DevState* state, double duv,
+                                    cudaStream_t s);
     // stw: stage twiddles of the length-N column FFT
     static cudaError_t cols(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
                             T* amp_out, long long s_row, long long s_col, int host_K, int host_r0, int host_W,

@@ -127,6 +127,50 @@ __global__ void __launch_bounds__(MAXT) cols_kernel(const C2<T>* __restrict__ zt
     }
 }
 
+// Column pass of a swept profile: the image is even in x and in y about its
+// centre, so every row transform is real (x (-1)^k) and every column of zt is
+// real and even about row N/2; its transform is real as well.  Two columns
+// k1 = 2p, k2 = 2p + 1 are therefore transformed together as the real and the
+// imaginary part of one complex column, and split after the transform:
+// FFT(a + i b) = FFT(a) + i FFT(b) with both transforms real.  Half the
+// column FFTs of cols_kernel.
+template <typename T, int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) cols_pair_kernel(const C2<T>* __restrict__ zt, int N, int band0, int band1,
+                                                         const C2<T>* __restrict__ stw, C2<T>* __restrict__ out,
+                                                         T* __restrict__ amp_out, long long s_row, long long s_col,
+                                                         const DevState* __restrict__ st) {
+    using CT = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    CT* buf = reinterpret_cast<CT*>(smem_raw);
+    const Window w = get_window(-1, -1, -1, st);
+    const int k1 = 2 * blockIdx.x, k2 = k1 + 1;
+    if (k1 >= w.K) return;  // uniform for the whole block
+    const bool two = k2 < w.K;
+    const CT* c1 = zt + (size_t)k1 * N;
+    const CT* c2 = zt + (size_t)k2 * N;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const bool in = i >= band0 && i < band1;
+        buf[sp(i)] = CT{in ? __ldg(&c1[i]).x : (T)0, (in && two) ? __ldg(&c2[i]).x : (T)0};
+    }
+    __syncthreads();
+    block_fft<T, E>(buf, N, ilog2(N), stw);
+    const int par1 = (k1 + N / 2) & 1;
+    for (int q = threadIdx.x; q < w.W; q += blockDim.x) {
+        const int r = w.r0 + q;
+        const CT x = buf[sp(r)];
+        const T f1 = ((r & 1) ^ par1) ? -x.x : x.x;
+        const long long o1 = (long long)q * s_row + (long long)k1 * s_col;
+        out[o1] = CT{f1, (T)0};
+        amp_out[o1] = fabs(f1);
+        if (two) {  // k2 has the opposite output-sign parity
+            const T f2 = ((r & 1) ^ par1) ? x.y : -x.y;
+            const long long o2 = (long long)q * s_row + (long long)k2 * s_col;
+            out[o2] = CT{f2, (T)0};
+            amp_out[o2] = fabs(f2);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // direct-DFT fallbacks for lengths the shared-memory FFT does not handle
 // (non powers of two, or too long for shared memory); tw has N entries.
@@ -688,6 +732,28 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
     rows_direct_kernel<T><<<nrows, 256, sm, s>>>(nullptr, N, N / 2 - rmax, intensity, nr, (T)Rmin, (T)dR, (T)dxy,
                                                  inv_cos, rmax, (T)central_value, 1, tw, zt, -1, state, duv, 1);
     return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::cols_profile(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
+                                    T* amp_out, long long s_row, long long s_col, const DevState* state, double duv,
+                                    cudaStream_t s) {
+    if (is_pow2(N) && N <= max_fft_n_impl<T>() && amp_out) {
+        const int C = N / 2 + 1;
+        FftCfg<T> c = fft_cfg<T>(N);
+        cudaError_t e = cudaSuccess;
+        GBG_DISPATCH_E(c.E, c.threads, {
+            auto kern = cols_pair_kernel<T, EE, TT>;
+            e = set_smem(kern, c.smem);
+            if (e == cudaSuccess) {
+                kern<<<(C + 1) / 2, c.threads, c.smem, s>>>(zt, N, band0, band1, stw, out, amp_out, s_row, s_col,
+                                                             state);
+                e = cudaGetLastError();
+            }
+        });
+        return e;
+    }
+    return cols(zt, N, band0, band1, tw, stw, out, amp_out, s_row, s_col, -1, -1, -1, state, duv, true, s);
 }
 
 template <typename T>
