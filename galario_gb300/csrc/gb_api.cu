@@ -347,11 +347,19 @@ template <typename T> struct Pipe {
             else
                 CK(L::cols_profile(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, st, duv, s));
         });
-        timed(c, s, ST_QUAD, [&] { CK(L::quads(win, amp, 1, N, C, st, quads, qcap, -1, -1, -1, s)); });
+        // a swept profile's spectrum is real: 4 real corners per cell record
+        const bool real_spec = img == nullptr;
+        timed(c, s, ST_QUAD, [&] {
+            if (real_spec)
+                CK(L::quads_real(win, 1, N, C, st, quads, qcap, s));
+            else
+                CK(L::quads(win, amp, 1, N, C, st, quads, qcap, -1, -1, -1, s));
+        });
         typename L::VisArgs a;
         a.spec = win;
         a.amp = amp;
         a.quads = quads;
+        a.real_quads = real_spec;
         a.quad_cap = qcap;
         a.phase_tab = c.phase_tab;
         a.s_row = 1;

@@ -120,6 +120,7 @@ template <typename T> struct Launch {
         const CT* spec;      // spectrum window
         const T* amp;        // |spec| in the same layout, or null (computed on the fly)
         const T* quads;      // cell-major records (see Launch::quads), or null: gather from spec/amp
+        bool real_quads = false;  // quads hold 4 real corners per cell (real spectrum of a swept profile)
         long long quad_cap;  // capacity of quads in cells; larger windows gather from spec/amp
         const double2* phase_tab;  // exp(2 pi i (j - PHASE_T/2) / PHASE_T), j in [0, PHASE_T]; FP64 path
         long long s_row, s_col;
@@ -170,6 +171,9 @@ template <typename T> struct Launch {
     static cudaError_t quads(const CT* spec, const T* amp, long long s_row, long long s_col, int C,
                              const DevState* state, T* quads, long long cap, int host_K, int host_r0, int host_W,
                              cudaStream_t s);
+    // records of a real spectrum: the 4 real corners of every cell (4 T per cell)
+    static cudaError_t quads_real(const CT* spec, long long s_row, long long s_col, int C, const DevState* state,
+                                  T* quads, long long cap, cudaStream_t s);
     static int vis_grid(int nd);
     // expert-stage kernels
     static cudaError_t fftshift_real(T* padded, int N, cudaStream_t s);

@@ -315,6 +315,39 @@ __device__ __forceinline__ bool interp_cell(const typename Launch<T>::VisArgs& a
     CT y[4];
     T am[4];
     const int qq = r0 - w.r0;
+    if (a.real_quads && (long long)w.K * w.W <= a.quad_cap) {
+        // real spectrum: z is real, so amp * exp(i sign_u arg z) = (amp sign(z), 0)
+        const bool inside = wrap ? (w.K == C && qq >= 0 && qq < w.W - 2) : (c0 < w.K - 1 && qq >= 0 && qq < w.W - 1);
+        if (!inside) {
+            *err |= ERR_WINDOW;
+            return false;
+        }
+        const T* rec = a.quads + ((long long)c0 * w.W + qq) * 4;
+        T yr[4];
+        if constexpr (sizeof(T) == 4) {
+            const float4 p0 = __ldg(reinterpret_cast<const float4*>(rec));
+            yr[0] = p0.x;
+            yr[1] = p0.y;
+            yr[2] = p0.z;
+            yr[3] = p0.w;
+        } else {
+            const double2 p0 = __ldg(reinterpret_cast<const double2*>(rec));
+            const double2 p1 = __ldg(reinterpret_cast<const double2*>(rec) + 1);
+            yr[0] = p0.x;
+            yr[1] = p0.y;
+            yr[2] = p1.x;
+            yr[3] = p1.y;
+        }
+        const T d1 = (yr[0] + yr[2]) - (yr[1] + yr[3]);
+        const T zr = t * (q * d1) + (t * (yr[1] - yr[0]) + q * (yr[3] - yr[0])) + yr[0];
+        const T m0 = fabs(yr[0]), m1 = fabs(yr[1]), m2 = fabs(yr[2]), m3 = fabs(yr[3]);
+        T amp = m0;
+        amp += (m3 - m0) * q;
+        amp += (m1 - m0) * t;
+        amp += (m0 - m1 + m2 - m3) * t * q;
+        *out = CT{zr < (T)0 ? -amp : amp, (T)0};
+        return true;
+    }
     if (a.quads && (long long)w.K * w.W <= a.quad_cap) {
         // one cell record: corners and moduli in 3 (FP32) or 6 (FP64) 16-byte loads
         const bool inside = wrap ? (w.K == C && qq >= 0 && qq < w.W - 2) : (c0 < w.K - 1 && qq >= 0 && qq < w.W - 1);
@@ -540,6 +573,30 @@ __global__ void quad_kernel(const C2<T>* __restrict__ spec, const T* __restrict_
             rec[2 * c + 1] = y.y;
             rec[8 + c] = amp[o];
         }
+    }
+}
+
+// Records of a real spectrum (a swept profile's): corner c of cell (k, q) at
+// quads[4 e + c], the moduli being their absolute values.
+template <typename T>
+__global__ void quad_real_kernel(const C2<T>* __restrict__ spec, long long s_row, long long s_col, int C,
+                                 const DevState* __restrict__ st, T* __restrict__ quads, long long cap) {
+    const Window w = get_window(-1, -1, -1, st);
+    const long long ncell = (long long)w.K * w.W;
+    if (ncell > cap) return;  // the visibility pass gathers from spec/amp instead
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e / w.W), q = (int)(e - (long long)k * w.W);
+        const bool wrap = (k + 1 == C);
+        const int rr[4] = {q, q + 1, wrap ? q + 2 : q + 1, wrap ? q + 1 : q};
+        const int cc[4] = {k, k, wrap ? 0 : k + 1, wrap ? 0 : k + 1};
+        bool ok = true;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) ok = ok && rr[c] < w.W && cc[c] < w.K;
+        if (!ok) continue;
+        T* rec = quads + e * 4;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) rec[c] = spec[(long long)rr[c] * s_row + (long long)cc[c] * s_col].x;
     }
 }
 
@@ -802,6 +859,13 @@ template <typename T> cudaError_t Launch<T>::vis(const VisArgs& args, cudaStream
     else if (chi2) vis_kernel<T, true, false><<<blocks, 256, 0, s>>>(a);
     else if (vo) vis_kernel<T, false, true><<<blocks, 256, 0, s>>>(a);
     else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::quads_real(const CT* spec, long long s_row, long long s_col, int C, const DevState* state,
+                                  T* q, long long cap, cudaStream_t s) {
+    quad_real_kernel<T><<<num_sms() * 4, 256, 0, s>>>(spec, s_row, s_col, C, state, q, cap);
     return cudaGetLastError();
 }
 
