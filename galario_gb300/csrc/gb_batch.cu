@@ -149,7 +149,8 @@ template <int E, int MAXT, int LG>
 __global__ void __launch_bounds__(MAXT) rows_batch_kernel(Geo g, int F, const float* __restrict__ intensity,
                                                           const ModelConst* __restrict__ mc,
                                                           const float2* __restrict__ tw,
-                                                          const float2* __restrict__ stw, float2* __restrict__ zt) {
+                                                          const float2* __restrict__ stw, void* __restrict__ zt_any,
+                                                          int real_out) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* buf = reinterpret_cast<float2*>(smem_raw);
     const int S = 2 * F + 1;                                  // staging row stride (odd: no bank conflicts)
@@ -197,15 +198,116 @@ __global__ void __launch_bounds__(MAXT) rows_batch_kernel(Geo g, int F, const fl
         }
     }
     __syncthreads();
-    float2* out = zt + (size_t)b * g.K * g.R;
+    // real_out: the swept image is even in x, so the row transforms are real
+    // (up to rounding); only the real parts are kept, as floats
     const int nrun = n0 + n1;
     const float inv_nrun = 1.f / i2f_small(nrun);
+    float2* out = static_cast<float2*>(zt_any) + (size_t)b * g.K * g.R;
+    float* outr = static_cast<float*>(zt_any) + (size_t)b * g.K * g.R;
     for (int e = threadIdx.x; e < g.K * nrun; e += blockDim.x) {
         int k, j;
         split_index(e, nrun, inv_nrun, &k, &j);
         const int row = j < n0 ? lo0 + j : lo1 + (j - n0);
         const int slot = j < n0 ? j : F + (j - n0);
-        out[(size_t)k * g.R + row] = stg[k * S + slot];
+        if (real_out) outr[(size_t)k * g.R + row] = stg[k * S + slot].x;
+        else out[(size_t)k * g.R + row] = stg[k * S + slot];
+    }
+}
+
+// Column pass of real, even columns (swept profiles): columns k1 = 2p and
+// k2 = 2p + 1 are the real and the imaginary part of one complex transform,
+// whose real and imaginary outputs are their (real) transforms.  Writes one
+// float per window element (output sign applied).
+template <int E, int MAXT, int LG>
+__global__ void __launch_bounds__(MAXT) cols_pair_batch_kernel(Geo g, const float* __restrict__ ztr,
+                                                               const float2* __restrict__ stw,
+                                                               float* __restrict__ wr) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* buf = reinterpret_cast<float2*>(smem_raw);
+    const int b = blockIdx.y, k1 = 2 * blockIdx.x, k2 = k1 + 1;
+    const bool two = k2 < g.K;
+    const float* c1 = ztr + ((size_t)b * g.K + k1) * g.R;
+    const float* c2 = c1 + g.R;
+    for (int i = threadIdx.x; i < g.N; i += blockDim.x) {
+        const int q = i - g.band0;
+        const bool in = q >= 0 && q < g.R;
+        buf[sp(i)] = make_float2(in ? __ldg(&c1[q]) : 0.f, (in && two) ? __ldg(&c2[q]) : 0.f);
+    }
+    __syncthreads();
+    block_fft_sel<float, E, LG>(buf, g.N, stw);
+    const int par1 = (k1 + g.N / 2) & 1;
+    float* w1 = wr + ((size_t)b * g.K + k1) * g.W;
+    float* w2 = w1 + g.W;
+    for (int q = threadIdx.x; q < g.W; q += blockDim.x) {
+        const int r = g.r0 + q;
+        const float2 x = buf[sp(r)];
+        const bool flip1 = ((r & 1) ^ par1) != 0;  // k2 has the opposite output-sign parity
+        w1[q] = flip1 ? -x.x : x.x;
+        if (two) w2[q] = flip1 ? x.y : -x.y;
+    }
+}
+
+// Cell gradients of a real window -> gradient of every element: the sum of
+// the corner sums of the (up to) four cells that have it as a corner, times
+// sign(y) (dchi2/dA -> dchi2/dy through |y|), times the output sign.  Grid (K, B).
+__global__ void quadT_real_kernel(Geo g, const float* __restrict__ cgrad4, const float* __restrict__ wr,
+                                  float* __restrict__ gwr) {
+    const long long ncell = (long long)g.K * g.W;
+    const int k = blockIdx.x, b = blockIdx.y;
+    const float* cg = cgrad4 + (size_t)b * ncell * 4;
+    for (int q = threadIdx.x; q < g.W; q += blockDim.x) {
+        float ga = 0.f;
+        auto take = [&](int kc, int qc, int c) {
+            if (kc < 0 || qc < 0 || kc >= g.K || qc >= g.W) return;
+            ga += cg[((long long)kc * g.W + qc) * 4 + c];
+        };
+        take(k, q, 0);
+        take(k, q - 1, 1);
+        take(k - 1, q - 1, 2);
+        take(k - 1, q, 3);
+        const size_t el = (size_t)b * ncell + (size_t)k * g.W + q;
+        const float y = wr[el];
+        float gy = y < 0.f ? -ga : (y > 0.f ? ga : 0.f);
+        const int row = g.r0 + q;
+        if (((row + k + g.N / 2) & 1)) gy = -gy;
+        gwr[el] = gy;
+    }
+}
+
+// Adjoint of cols_pair_batch_kernel.  The forward keeps the real part of the
+// transform of a real column, whose adjoint is Re(FFT(g)); only its part even
+// about row N/2 matters (the row adjoint adds mirror rows), and that is the
+// transform of the even part of g, which is real: so two columns again share
+// one complex transform.  Writes (value, 0) per band row, the row adjoint's
+// complex layout.
+template <int E, int MAXT, int LG>
+__global__ void __launch_bounds__(MAXT) colsT_pair_batch_kernel(Geo g, const float* __restrict__ gwr,
+                                                                const float2* __restrict__ stw,
+                                                                float2* __restrict__ zbar) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* buf = reinterpret_cast<float2*>(smem_raw);
+    const int b = blockIdx.y, k1 = 2 * blockIdx.x, k2 = k1 + 1;
+    const bool two = k2 < g.K;
+    const float* c1 = gwr + ((size_t)b * g.K + k1) * g.W;
+    const float* c2 = c1 + g.W;
+    auto at = [&](const float* c, int r) {  // element of window row r (0 outside the window)
+        const int q = r - g.r0;
+        return (q >= 0 && q < g.W) ? __ldg(&c[q]) : 0.f;
+    };
+    for (int i = threadIdx.x; i < g.N; i += blockDim.x) {
+        const int m = (g.N - i) & (g.N - 1);
+        const float e1 = 0.5f * (at(c1, i) + at(c1, m));
+        const float e2 = two ? 0.5f * (at(c2, i) + at(c2, m)) : 0.f;
+        buf[sp(i)] = make_float2(e1, e2);
+    }
+    __syncthreads();
+    block_fft_sel<float, E, LG>(buf, g.N, stw);
+    float2* o1 = zbar + ((size_t)b * g.K + k1) * g.R;
+    float2* o2 = o1 + g.R;
+    for (int q = threadIdx.x; q < g.R; q += blockDim.x) {
+        const float2 x = buf[sp(g.band0 + q)];
+        o1[q] = make_float2(x.x, 0.f);
+        if (two) o2[q] = make_float2(x.y, 0.f);
     }
 }
 
@@ -362,8 +464,10 @@ __device__ __forceinline__ DF df_dot2(float x, DF a, float y, DF b) {
 // dataset holds only finite (u, v).  The cell indices are still clamped to
 // the window, so that no access can leave it; a clamp that changes an index
 // raises ERR_WINDOW.
-__device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, const float4* __restrict__ wel_b,
-                                           float u, float v, PointEval& p) {
+// rotation, cell index and fractions of one (visibility, model); returns the
+// clamped cell (c0, q0) of the column-major window
+__device__ __forceinline__ void locate_point(const Geo& g, const ModelConst& m, float u, float v, PointEval& p,
+                                             int* c0, int* q0) {
     p.err = 0u;
     // rotated coordinates in grid units: a = u'/duv, c = v'/duv
     const DF a = df_dot2(u, m.cu, -v, m.sv);
@@ -386,6 +490,32 @@ __device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, co
     const int c0c = min(max(fu, 0), g.K - 2), qqc = min(max(qq, 0), g.W - 2);
     if (c0c != fu || qqc != qq) p.err = ERR_WINDOW;
     p.cell = c0c * g.W + qqc;
+    *c0 = c0c;
+    *q0 = qqc;
+}
+
+// V = U exp(2 pi i (u dRA + v dDec)) (the rotation-invariant form of the phase)
+__device__ __forceinline__ void apply_phase_point(const ModelConst& m, float u, float v, float2 U, PointEval& p) {
+    p.pc = 1.f;
+    p.ps = 0.f;
+    if (m.phase) {
+        // u'dRA' + v'dDec' = u dRA + v dDec (both pairs rotated by PA)
+        const DF ph = df_dot2(u, m.dra, v, m.ddec);
+        float n;
+        if (fabsf(ph.hi) < 4194304.f) rint_i(ph.hi, &n);
+        else n = rintf(ph.hi);
+        const float f = __fadd_rn(__fsub_rn(ph.hi, n), ph.lo);
+        sincos2pi_f32(f, &p.ps, &p.pc);
+        U = make_float2(U.x * p.pc - U.y * p.ps, U.x * p.ps + U.y * p.pc);
+    }
+    p.V = U;
+}
+
+__device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, const float4* __restrict__ wel_b,
+                                           float u, float v, PointEval& p) {
+    int c0c, qqc;
+    locate_point(g, m, u, v, p, &c0c, &qqc);
+    const float su = p.su;
     // corners of cell (k, q): (k, q), (k, q+1), (k+1, q+1), (k+1, q) of the
     // column-major window (no wrap: K < N/2 + 1 by the host's uv-range check)
     const float4* e0 = wel_b + (size_t)c0c * g.W + qqc;
@@ -415,20 +545,37 @@ __device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, co
         cph = p.zr * p.rn;
         sph = su * p.zi * p.rn;
     }
-    float2 U = make_float2(A * cph, A * sph);
-    p.pc = 1.f;
-    p.ps = 0.f;
-    if (m.phase) {
-        // u'dRA' + v'dDec' = u dRA + v dDec (both pairs rotated by PA)
-        const DF ph = df_dot2(u, m.dra, v, m.ddec);
-        float n;
-        if (fabsf(ph.hi) < 4194304.f) rint_i(ph.hi, &n);
-        else n = rintf(ph.hi);
-        const float f = __fadd_rn(__fsub_rn(ph.hi, n), ph.lo);
-        sincos2pi_f32(f, &p.ps, &p.pc);
-        U = make_float2(U.x * p.pc - U.y * p.ps, U.x * p.ps + U.y * p.pc);
-    }
-    p.V = U;
+    apply_phase_point(m, u, v, make_float2(A * cph, A * sph), p);
+}
+
+// The spectrum of a swept profile is real (the image is even in x and y):
+// the window holds one real per element, z is real and
+// amp * exp(i sign_u arg z) = (amp * sign(z), 0).  p.y[c].x are the corners,
+// p.am[c] their moduli, p.zr = z, p.rn = sign(z).
+__device__ __forceinline__ void eval_point_real(const Geo& g, const ModelConst& m, const float* __restrict__ wr_b,
+                                                float u, float v, PointEval& p) {
+    int c0c, qqc;
+    locate_point(g, m, u, v, p, &c0c, &qqc);
+    const float* e0 = wr_b + (size_t)c0c * g.W + qqc;
+    const float y0 = __ldg(e0), y1 = __ldg(e0 + 1), y2 = __ldg(e0 + g.W + 1), y3 = __ldg(e0 + g.W);
+    p.y[0].x = y0;
+    p.y[1].x = y1;
+    p.y[2].x = y2;
+    p.y[3].x = y3;
+    p.am[0] = fabsf(y0);
+    p.am[1] = fabsf(y1);
+    p.am[2] = fabsf(y2);
+    p.am[3] = fabsf(y3);
+    const float t = p.t, q = p.q;
+    const float d1 = (y0 + y2) - (y1 + y3);
+    p.zr = t * (q * d1) + (t * (y1 - y0) + q * (y3 - y0)) + y0;
+    float A = p.am[0];
+    A += (p.am[3] - p.am[0]) * q;
+    A += (p.am[1] - p.am[0]) * t;
+    A += (p.am[0] - p.am[1] + p.am[2] - p.am[3]) * t * q;
+    p.A = A;
+    p.rn = p.zr < 0.f ? -1.f : 1.f;
+    apply_phase_point(m, u, v, make_float2(A * p.rn, 0.f), p);
 }
 
 // Accumulators per model and block: chi2, dPA, dRA, dDec
@@ -478,6 +625,18 @@ __device__ __forceinline__ void emit_cell(float* __restrict__ cg, int cell, cons
 }
 constexpr int kFirstStride = 13;  // shared-memory slot of a thread's first run (odd: no bank conflicts)
 
+// real windows: the moments of dchi2/dA give the 4 corner sums of the cell,
+// added to its 4-float record with one 16-byte atomic
+__device__ __forceinline__ void emit_cell_real(float* __restrict__ cg, int cell, const float* M) {
+    const float m1 = M[0], mt = M[1], mq = M[2], mtq = M[3];
+    atomicAdd(reinterpret_cast<float4*>(cg + (size_t)cell * 4),
+              make_float4((m1 - mt) - (mq - mtq), mt - mtq, mtq, mq - mtq));
+}
+template <bool REAL> __device__ __forceinline__ void emit_run(float* __restrict__ cg, int cell, const float* M) {
+    if constexpr (REAL) emit_cell_real(cg, cell, M);
+    else emit_cell(cg, cell, M);
+}
+
 // Grid: x = blocks of kVisThreads * PTS visibilities, y = groups of Bg
 // models.  The hardware issues the x blocks of one group before the next, so
 // the windows (and gradient records) of about Bg models are live in L2 at a time.
@@ -490,14 +649,16 @@ constexpr int kFirstStride = 13;  // shared-memory slot of a thread's first run 
 // first run, when it continues the previous lane's last run, is handed to that
 // lane; the last runs then go through one warp-segmented reduction (shuffles)
 // and one lane per run of equal cells adds it.
-template <bool GRAD, int PTS>
+// REAL: the window is real (swept profiles): one float per element, one
+// gradient component (dchi2/dA) per corner, 4-float cell records.
+template <bool GRAD, int PTS, bool REAL>
 __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, int Bg, int nd, const float* __restrict__ u,
                                                                 const float* __restrict__ v,
                                                                 const float* __restrict__ re,
                                                                 const float* __restrict__ im,
                                                                 const float* __restrict__ w,
                                                                 const ModelConst* __restrict__ mc,
-                                                                const float4* __restrict__ wel,
+                                                                const void* __restrict__ wel_any,
                                                                 float* __restrict__ cgrad, double* __restrict__ partials,
                                                                 DevState* st) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -509,7 +670,12 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
     float* wacc = reinterpret_cast<float*>(smc + Bg);
     // each thread's first run of equal cells (moments), read by the previous lane
     float* fst_all = wacc + Bg * kAcc * kVisWarps;
-    float* fst = fst_all + threadIdx.x * kFirstStride;
+    constexpr int NR = REAL ? 4 : 12;              // floats of a run's moments
+    constexpr int FS = REAL ? 5 : kFirstStride;   // odd slot stride: no bank conflicts
+    float* fst = fst_all + threadIdx.x * FS;
+    const float4* wel = static_cast<const float4*>(wel_any);
+    const float* welr = static_cast<const float*>(wel_any);
+    constexpr int kRecF = REAL ? 4 : kGRec;       // floats per gradient cell record
     for (int i = threadIdx.x; i < nb; i += blockDim.x) smc[i] = mc[b0 + i];
     // this thread's points
     float pu[PTS], pv[PTS], pre[PTS], pim[PTS], pw[PTS];
@@ -526,13 +692,12 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
     for (int bl = 0; bl < nb; ++bl) {
         const int b = b0 + bl;
         const ModelConst m = smc[bl];
-        const float4* qb = wel + (size_t)b * ncell;
-        float* cg = cgrad + (size_t)b * ncell * kGRec;
+        float* cg = cgrad + (size_t)b * ncell * kRecF;
         float acc[kAcc] = {0.f, 0.f, 0.f, 0.f};
-        float run[12];  // moments of the open run of equal cells
+        float run[NR];  // moments of the open run of equal cells
         int cur = -1, fcell = -1;
 #pragma unroll
-        for (int cc = 0; cc < 12; ++cc) run[cc] = 0.f;
+        for (int cc = 0; cc < NR; ++cc) run[cc] = 0.f;
 #pragma unroll
         for (int j = 0; j < PTS; ++j) {
             const bool live = pw[j] != 0.f;  // w = 0: padding (or a zero-weight visibility)
@@ -540,7 +705,8 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
             p.cell = -1;
             p.V = make_float2(0.f, 0.f);
             if (live) {
-                eval_point(g, m, qb, pu[j], pv[j], p);
+                if constexpr (REAL) eval_point_real(g, m, welr + (size_t)b * ncell, pu[j], pv[j], p);
+                else eval_point(g, m, wel + (size_t)b * ncell, pu[j], pv[j], p);
                 err |= p.err;
             }
             const float dr = p.V.x - pre[j], di = p.V.y - pim[j];
@@ -552,50 +718,64 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
                 const float dphi = -(gx * p.V.y - gy * p.V.x);
                 acc[2] += dphi * 6.28318530717958647692f * pu[j];
                 acc[3] += dphi * 6.28318530717958647692f * pv[j];
-                // G_U = G conj(P)
-                const float gux = gx * p.pc + gy * p.ps, guy = -gx * p.ps + gy * p.pc;
-                // U = A * (zr, su zi) / |z|
-                const float ex = p.zr * p.rn, ey = p.zi * p.rn;  // e = z/|z|
-                const float gA = gux * ex + guy * (p.su * ey);
-                // gradient w.r.t. e (undo the conjugation for u < 0)
-                const float gex = p.A * gux, gey = p.su * p.A * guy;
-                const float dot = ex * gex + ey * gey;
-                const float gzx = (gex - ex * dot) * p.rn, gzy = (gey - ey * dot) * p.rn;
                 const float t = p.t, q = p.q;
-                // position: q = |a|, t = N/2 + vo su c with a = u'/duv, c = v'/duv;
-                // da/dPA = -c, dc/dPA = a
-                const float dzqx = (p.y[3].x - p.y[0].x) + t * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
-                const float dzqy = (p.y[3].y - p.y[0].y) + t * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
-                const float dztx = (p.y[1].x - p.y[0].x) + q * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
-                const float dzty = (p.y[1].y - p.y[0].y) + q * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
-                const float dAq = (p.am[3] - p.am[0]) + t * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
-                const float dAt = (p.am[1] - p.am[0]) + q * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
-                const float gq = gzx * dzqx + gzy * dzqy + gA * dAq;
-                const float gt = gzx * dztx + gzy * dzty + gA * dAt;
+                float gv[NR], dAq, dAt, gq, gt;
+                if constexpr (REAL) {
+                    // U = (A s, 0), s = sign(z): only the modulus path carries a gradient
+                    const float gA = (gx * p.pc + gy * p.ps) * p.rn;
+                    gv[0] = gA;
+                    dAq = (p.am[3] - p.am[0]) + t * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
+                    dAt = (p.am[1] - p.am[0]) + q * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
+                    gq = gA * dAq;
+                    gt = gA * dAt;
+                } else {
+                    // G_U = G conj(P)
+                    const float gux = gx * p.pc + gy * p.ps, guy = -gx * p.ps + gy * p.pc;
+                    // U = A * (zr, su zi) / |z|
+                    const float ex = p.zr * p.rn, ey = p.zi * p.rn;  // e = z/|z|
+                    const float gA = gux * ex + guy * (p.su * ey);
+                    // gradient w.r.t. e (undo the conjugation for u < 0)
+                    const float gex = p.A * gux, gey = p.su * p.A * guy;
+                    const float dot = ex * gex + ey * gey;
+                    const float gzx = (gex - ex * dot) * p.rn, gzy = (gey - ey * dot) * p.rn;
+                    // position: q = |a|, t = N/2 + vo su c with a = u'/duv, c = v'/duv;
+                    // da/dPA = -c, dc/dPA = a
+                    const float dzqx = (p.y[3].x - p.y[0].x) + t * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
+                    const float dzqy = (p.y[3].y - p.y[0].y) + t * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
+                    const float dztx = (p.y[1].x - p.y[0].x) + q * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
+                    const float dzty = (p.y[1].y - p.y[0].y) + q * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
+                    dAq = (p.am[3] - p.am[0]) + t * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
+                    dAt = (p.am[1] - p.am[0]) + q * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
+                    gq = gzx * dzqx + gzy * dzqy + gA * dAq;
+                    gt = gzx * dztx + gzy * dzty + gA * dAt;
+                    gv[0] = gzx;
+                    gv[1] = gzy;
+                    gv[2] = gA;
+                }
                 acc[1] += gq * (p.su * (-p.vr)) + gt * (g.vo * p.su * p.ur);
                 // runs of equal cells within the thread, summed as moments in registers
-                const float gv[3] = {gzx, gzy, gA};
+                constexpr int NC = NR / 4;  // gradient components per corner
                 const float mom[4] = {1.f, t, q, t * q};
                 if (p.cell == cur) {
 #pragma unroll
                     for (int mm = 0; mm < 4; ++mm)
 #pragma unroll
-                        for (int i = 0; i < 3; ++i) run[3 * mm + i] = fmaf(gv[i], mom[mm], run[3 * mm + i]);
+                        for (int i = 0; i < NC; ++i) run[NC * mm + i] = fmaf(gv[i], mom[mm], run[NC * mm + i]);
                 } else {
                     if (cur >= 0) {
                         if (fcell < 0) {
                             fcell = cur;
 #pragma unroll
-                            for (int cc = 0; cc < 12; ++cc) fst[cc] = run[cc];
+                            for (int cc = 0; cc < NR; ++cc) fst[cc] = run[cc];
                         } else {
-                            emit_cell(cg, cur, run);  // begins and ends inside this thread
+                            emit_run<REAL>(cg, cur, run);  // begins and ends inside this thread
                         }
                     }
                     cur = p.cell;
 #pragma unroll
                     for (int mm = 0; mm < 4; ++mm)
 #pragma unroll
-                        for (int i = 0; i < 3; ++i) run[3 * mm + i] = gv[i] * mom[mm];
+                        for (int i = 0; i < NC; ++i) run[NC * mm + i] = gv[i] * mom[mm];
                 }
             }
         }
@@ -608,11 +788,11 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
             __syncwarp();
             const bool take = __shfl_down_sync(full, (int)pass, 1) && lane < 31;
             if (take) {
-                const float* nf = fst + kFirstStride;  // the next lane's slot
+                const float* nf = fst + FS;  // the next lane's slot
 #pragma unroll
-                for (int cc = 0; cc < 12; ++cc) run[cc] += nf[cc];
+                for (int cc = 0; cc < NR; ++cc) run[cc] += nf[cc];
             }
-            if (fcell >= 0 && !pass) emit_cell(cg, fcell, fst);
+            if (fcell >= 0 && !pass) emit_run<REAL>(cg, fcell, fst);
             // last runs: lanes with equal keys are consecutive; reduce each
             // segment with shuffles, then its first lane adds it
             const unsigned heads = __ballot_sync(full, lane == 0 || klast != kprev);
@@ -625,13 +805,13 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
                 for (int d = 1; d < maxlen; d <<= 1) {
                     const int seg_d = __shfl_down_sync(full, seg, d);
 #pragma unroll
-                    for (int cc = 0; cc < 12; ++cc) {
+                    for (int cc = 0; cc < NR; ++cc) {
                         const float o = __shfl_down_sync(full, run[cc], d);
                         if (lane + d < 32 && seg_d == seg) run[cc] += o;
                     }
                 }
             }
-            if (cur >= 0 && ((heads >> lane) & 1u)) emit_cell(cg, cur, run);
+            if (cur >= 0 && ((heads >> lane) & 1u)) emit_run<REAL>(cg, cur, run);
             __syncwarp();  // the slots are rewritten for the next model
         }
         // warp sums of this model's accumulators
@@ -1632,13 +1812,16 @@ static void batch_run(const BatchCall& call) {
         if (ncoef) BCK(cudaMemcpyAsync(coef_d, coef.data(), sizeof(double) * ncoef, cudaMemcpyHostToDevice, s));
         DevState* st = ws.state.get<DevState>(1);
         BCK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
-        float* cgrad = grad ? ws.cgrad.get<float>((size_t)B * ncell * kGRec) : nullptr;
+        // swept profiles have a real spectrum: real window, 4-float gradient records
+        const bool real = !image;
+        const int recf = real ? 4 : kGRec;
+        float* cgrad = grad ? ws.cgrad.get<float>((size_t)B * ncell * recf) : nullptr;
         float2* gwin = grad ? ws.gwin.get<float2>((size_t)B * ncell) : nullptr;
         float2* zbar = grad ? ws.zbar.get<float2>((size_t)B * g.K * g.R) : nullptr;
         double* ginc_d = grad ? ws.gI_tmp.get<double>((size_t)B) : nullptr;
         float* gcentral = grad ? ws.gcentral.get<float>((size_t)B) : nullptr;
         // models per group of the vis pass: the group's windows and gradient records within ~64 MiB of L2
-        const double rec_bytes = (double)ncell * (sizeof(float4) + (grad ? kGRec * sizeof(float) : 0));
+        const double rec_bytes = (double)ncell * ((real ? sizeof(float) : sizeof(float4)) + (grad ? recf * sizeof(float) : 0));
         int Bg = (int)std::floor(64.0 * 1024 * 1024 / rec_bytes);
         if (Bg < 1) Bg = 1;
         if (Bg > B) Bg = B;
@@ -1675,12 +1858,12 @@ static void batch_run(const BatchCall& call) {
             GBB_DISPATCH_E(E, g.M, {
                 BCK((cudaError_t)smem_attr((const void*)rows_batch_kernel<EE, TT, LG>, sm));
                 rows_batch_kernel<EE, TT, LG><<<dim3((g.rmax + Frows) / Frows, B), fft_threads(g.M, EE), sm, s>>>(
-                    g, Frows, intensity, mc, tws.first, ws.stage_tw(g.M, EE), zt);
+                    g, Frows, intensity, mc, tws.first, ws.stage_tw(g.M, EE), (void*)zt, real ? 1 : 0);
             });
             BCK(cudaGetLastError());
         };
         // column pass shape: E values per thread, + kTmaCols for the TMA-fed persistent variant
-        const bool tma_ok = (g.R % 2 == 0) &&
+        const bool tma_ok = !real && (g.R % 2 == 0) &&
                             sizeof(float2) * (2 * (size_t)g.R + fft_slots(g.N)) + 16 <= 200 * 1024;
         auto cols = [&](int shape) {
             const int E = shape % kTmaCols;
@@ -1701,6 +1884,15 @@ static void batch_run(const BatchCall& call) {
                 return;
             }
             const size_t sm = sizeof(float2) * fft_slots(g.N);
+            if (real) {
+                GBB_DISPATCH_E(E, g.N, {
+                    BCK((cudaError_t)smem_attr((const void*)cols_pair_batch_kernel<EE, TT, LG>, sm));
+                    cols_pair_batch_kernel<EE, TT, LG><<<dim3((g.K + 1) / 2, B), fft_threads(g.N, EE), sm, s>>>(
+                        g, reinterpret_cast<const float*>(zt), ws.stage_tw(g.N, EE), reinterpret_cast<float*>(wel));
+                });
+                BCK(cudaGetLastError());
+                return;
+            }
             GBB_DISPATCH_E(E, g.N, {
                 BCK((cudaError_t)smem_attr((const void*)cols_batch_kernel<EE, TT, LG>, sm));
                 cols_batch_kernel<EE, TT, LG><<<dim3(g.K, B), fft_threads(g.N, EE), sm, s>>>(
@@ -1711,20 +1903,31 @@ static void batch_run(const BatchCall& call) {
         auto vis = [&](int pts) {
             const int vb = (int)((d->nd_pad + (long long)kVisThreads * pts - 1) / ((long long)kVisThreads * pts));
             const size_t vsm = sizeof(ModelConst) * Bg + sizeof(float) * Bg * kAcc * kVisWarps +
-                               (grad ? sizeof(float) * kVisThreads * kFirstStride : 0);
+                               (grad ? sizeof(float) * kVisThreads * (real ? 5 : kFirstStride) : 0);
             const dim3 grid(vb, ngroups);
-#define GBB_VIS(G_, P_)                                                                                        \
+#define GBB_VIS(G_, P_, R_)                                                                                    \
     do {                                                                                                       \
-        BCK((cudaError_t)smem_attr((const void*)vis_batch_kernel<G_, P_>, vsm));                               \
-        vis_batch_kernel<G_, P_><<<grid, kVisThreads, vsm, s>>>(g, B, Bg, d->nd_pad, d->u, d->v, d->re, d->im,\
-                                                               d->w, mc, wel, cgrad, partials, st);            \
+        BCK((cudaError_t)smem_attr((const void*)vis_batch_kernel<G_, P_, R_>, vsm));                           \
+        vis_batch_kernel<G_, P_, R_><<<grid, kVisThreads, vsm, s>>>(g, B, Bg, d->nd_pad, d->u, d->v, d->re,   \
+                                                                   d->im, d->w, mc, (const void*)wel, cgrad,  \
+                                                                   partials, st);                             \
     } while (0)
-            if (grad) {
-                if (pts == 2) GBB_VIS(true, 2);
-                else GBB_VIS(true, 4);
+            if (real) {
+                if (grad) {
+                    if (pts == 2) GBB_VIS(true, 2, true);
+                    else GBB_VIS(true, 4, true);
+                } else {
+                    if (pts == 2) GBB_VIS(false, 2, true);
+                    else GBB_VIS(false, 4, true);
+                }
             } else {
-                if (pts == 2) GBB_VIS(false, 2);
-                else GBB_VIS(false, 4);
+                if (grad) {
+                    if (pts == 2) GBB_VIS(true, 2, false);
+                    else GBB_VIS(true, 4, false);
+                } else {
+                    if (pts == 2) GBB_VIS(false, 2, false);
+                    else GBB_VIS(false, 4, false);
+                }
             }
 #undef GBB_VIS
             BCK(cudaGetLastError());
@@ -1732,6 +1935,15 @@ static void batch_run(const BatchCall& call) {
         };
         auto colsT = [&](int E) {
             const size_t sm = sizeof(float2) * fft_slots(g.N);
+            if (real) {
+                GBB_DISPATCH_E(E, g.N, {
+                    BCK((cudaError_t)smem_attr((const void*)colsT_pair_batch_kernel<EE, TT, LG>, sm));
+                    colsT_pair_batch_kernel<EE, TT, LG><<<dim3((g.K + 1) / 2, B), fft_threads(g.N, EE), sm, s>>>(
+                        g, reinterpret_cast<const float*>(gwin), ws.stage_tw(g.N, EE), zbar);
+                });
+                BCK(cudaGetLastError());
+                return;
+            }
             GBB_DISPATCH_E(E, g.N, {
                 BCK((cudaError_t)smem_attr((const void*)colsT_batch_kernel<EE, TT, LG>, sm));
                 colsT_batch_kernel<EE, TT, LG><<<dim3(g.K, B), fft_threads(g.N, EE), sm, s>>>(
@@ -1762,7 +1974,7 @@ static void batch_run(const BatchCall& call) {
             BCK(cudaGetLastError());
         };
         auto zero_grads = [&] {
-            BCK(cudaMemsetAsync(cgrad, 0, sizeof(float) * (size_t)B * ncell * kGRec, s));
+            BCK(cudaMemsetAsync(cgrad, 0, sizeof(float) * (size_t)B * ncell * recf, s));
             BCK(cudaMemsetAsync(ginc_d, 0, sizeof(double) * B, s));
             BCK(cudaMemsetAsync(gcentral, 0, sizeof(float) * B, s));
             if (!image) BCK(cudaMemsetAsync(grad_intensity, 0, sizeof(float) * (size_t)B * nr, s));
@@ -1784,7 +1996,11 @@ static void batch_run(const BatchCall& call) {
             BCK(cudaGetLastError());
             if (!grad) return;
             // ---- adjoint ----
-            quadT_batch_kernel<<<dim3(g.K, B), 256, 0, s>>>(g, cgrad, wel, gwin);
+            if (real)
+                quadT_real_kernel<<<dim3(g.K, B), 256, 0, s>>>(g, cgrad, reinterpret_cast<const float*>(wel),
+                                                               reinterpret_cast<float*>(gwin));
+            else
+                quadT_batch_kernel<<<dim3(g.K, B), 256, 0, s>>>(g, cgrad, wel, gwin);
             BCK(cudaGetLastError());
             colsT(sh.e_colsT);
             rowsT(sh.e_rowsT);
