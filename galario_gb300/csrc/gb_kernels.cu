@@ -22,6 +22,9 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <cstdint>
+#include <type_traits>
+
 #include "gb_device.cuh"
 #include "gb_internal.cuh"
 
@@ -258,14 +261,40 @@ __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, 
     // flagged by the visibility pass); the window adds a relative margin
     // larger than the float rounding of this maximum
     T mt = (T)0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += gridDim.x * blockDim.x) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    int done = 0;
+    if ((reinterpret_cast<uintptr_t>(u) & 15) == 0 && (reinterpret_cast<uintptr_t>(v) & 15) == 0) {
+        // 16-byte vector loads, two vectors of each array in flight per thread
+        using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+        constexpr int L = 16 / sizeof(T);
+        const int nvec = nd / L;
+        const V* uv = reinterpret_cast<const V*>(u);
+        const V* vv = reinterpret_cast<const V*>(v);
+        auto acc = [&](const V& a, const V& b) {
+            if constexpr (sizeof(T) == 4) {
+                mt = fmax(mt, fmax(fmax(a.x * a.x + b.x * b.x, a.y * a.y + b.y * b.y),
+                                   fmax(a.z * a.z + b.z * b.z, a.w * a.w + b.w * b.w)));
+            } else {
+                mt = fmax(mt, fmax(a.x * a.x + b.x * b.x, a.y * a.y + b.y * b.y));
+            }
+        };
+        int i = tid;
+        for (; i + nth < nvec; i += 2 * nth) {
+            const V a0 = __ldg(&uv[i]), b0 = __ldg(&vv[i]), a1 = __ldg(&uv[i + nth]), b1 = __ldg(&vv[i + nth]);
+            acc(a0, b0);
+            acc(a1, b1);
+        }
+        if (i < nvec) acc(__ldg(&uv[i]), __ldg(&vv[i]));
+        done = nvec * L;
+    }
+    for (int i = done + tid; i < nd; i += nth) {
         const T a = __ldg(&u[i]), b = __ldg(&v[i]);
         mt = fmax(mt, a * a + b * b);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mt = fmax(mt, __shfl_xor_sync(0xffffffffu, mt, o));
     double m = (double)mt;
-    __shared__ double sh[32];
+    __shared__ double sh[32];  // one per warp, blocks of up to 1024 threads
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -711,7 +740,7 @@ template <typename T> int Launch<T>::max_fft_n() { return max_fft_n_impl<T>(); }
 template <typename T>
 cudaError_t Launch<T>::extent(const T* u, const T* v, int nd, int N, double duv, DevState* state, cudaStream_t s) {
     int blocks = (nd + 255) / 256;
-    const int cap = num_sms() * 4;
+    const int cap = num_sms() * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
     extent_kernel<T><<<blocks, 256, 0, s>>>(u, v, nd, N, duv, state);
