@@ -265,3 +265,31 @@ def test_batch_rejects_uv_beyond_image(case):
     u[5] = np.nan
     with pytest.raises(ValueError, match="must be finite"):
         Dataset(u, c["v"], c["re"], c["im"], c["w"])
+
+
+def test_batch_profile_wider_than_image(oracle_port):
+    """Batched path with the profile support beyond the image (rmax = nxy/2)."""
+    import torch
+    from galario_gb300.batch import Dataset, chi2_profile_batch, status
+    nxy, dxy = 256, 0.02 * arcsec
+    Rmin, dR, nr = 1e-4 * arcsec, 1e-3 * arcsec, 4000
+    R = Rmin + dR * np.arange(nr)
+    I = np.stack([1e10 * np.exp(-0.5 * (R / (1.5 * arcsec)) ** 2), 5e9 * np.exp(-0.5 * (R / (2.5 * arcsec)) ** 2)])
+    I = I.astype(np.float32).astype(np.float64)
+    duv = 1 / (nxy * dxy)
+    u, v = uv_log_uniform(5000, 0.5 * duv, 0.45 * nxy / 2 * duv, seed=7)
+    rng = np.random.default_rng(8)
+    re, im, w = rng.normal(0, 1e-3, 5000), rng.normal(0, 1e-3, 5000), rng.uniform(0.5, 2, 5000) * 1e6
+    c = {k: np.asarray(x, dtype=np.float32).astype(np.float64) for k, x in dict(u=u, v=v, re=re, im=im, w=w).items()}
+    params = np.array([[0.3, 1.0, 0.01 * arcsec, 0.0], [0.6, 2.0, 0.0, -0.02 * arcsec]]).astype(np.float32)
+    ds = Dataset(c["u"], c["v"], c["re"], c["im"], c["w"])
+    chi2 = chi2_profile_batch(ds, torch.tensor(I, dtype=torch.float32, device="cuda"),
+                              torch.tensor(params, device="cuda"), Rmin, dR, dxy, nxy).cpu().numpy()
+    assert status() == 0
+    orc = oracle_port.get("port", "double")
+    f = lambda x: float(np.float32(x))  # noqa: E731
+    for b in range(2):
+        inc, PA, dRA, dDec = (float(x) for x in params[b])
+        ref = orc.chi2Profile(I[b], f(Rmin), f(dR), nxy, f(dxy), c["u"], c["v"], c["re"], c["im"], c["w"], inc=inc,
+                              PA=PA, dRA=dRA, dDec=dDec)
+        assert abs(chi2[b] - ref) / ref <= CHI2_TOL, (b, chi2[b], ref)

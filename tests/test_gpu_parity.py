@@ -107,6 +107,28 @@ def test_profile_double(g, orc, inc, PA, dRA, dDec):
     assert abs(cg - co) / abs(co) <= DP_CHI2
 
 
+@pytest.mark.parametrize("nxy", [256, 250])
+def test_profile_wider_than_image(g, orc, nxy):
+    """Profile support beyond the image (rmax clamped to nxy/2: the edge row and
+    column carry emission) and a non power of two size: the symmetric-profile
+    shortcuts (shared mirror rows, paired real columns, real spectrum) must
+    still match the oracle."""
+    dxy = 0.02 * arcsec
+    Rmin, dR, nr = 1e-4 * arcsec, 1e-3 * arcsec, 4000  # extent 4", image half-width 2.5"
+    R = Rmin + dR * np.arange(nr)
+    I = 1e10 * np.exp(-0.5 * (R / (1.5 * arcsec)) ** 2)
+    duv = 1 / (nxy * dxy)
+    u, v = uv_log_uniform(5000, 0.5 * duv, 0.45 * nxy / 2 * duv, seed=5)
+    re, im, w = _obs(5000, seed=6)
+    kw = dict(inc=35 * deg, PA=1.2, dRA=0.03 * arcsec, dDec=-0.01 * arcsec)
+    vg = g.double.sampleProfile(I, Rmin, dR, nxy, dxy, u, v, **kw)
+    vo = orc["double"].sampleProfile(I, Rmin, dR, nxy, dxy, u, v, **kw)
+    assert rel_max(vg, vo) <= DP_V
+    cg = g.double.chi2Profile(I, Rmin, dR, nxy, dxy, u, v, re, im, w, **kw)
+    co = orc["double"].chi2Profile(I, Rmin, dR, nxy, dxy, u, v, re, im, w, **kw)
+    assert abs(cg - co) / abs(co) <= DP_CHI2
+
+
 def test_sweep_double(g, orc):
     Rmin, dR, nr = 1e-6 * arcsec, 0.001 * arcsec, 2000
     dxy = 0.2 * arcsec
