@@ -278,3 +278,23 @@ def test_uv_wrap_and_outside_spectrum(g, orc):
     # the context stays usable afterwards
     out = g.double.sampleImage(img, dxy, u[:1].copy(), v[:1].copy())
     assert np.isfinite(out).all()
+
+
+def test_concurrent_host_threads(g):
+    """Calls from several host threads (ctypes releases the GIL) are serialised
+    per device by the library and give the same results as sequential calls."""
+    from concurrent.futures import ThreadPoolExecutor
+    nxy, dxy = 512, 0.01 * arcsec
+    Rmin, dR, nr = 1e-4 * arcsec, 5e-4 * arcsec, 2000
+    R = Rmin + dR * np.arange(nr)
+    duv = 1 / (nxy * dxy)
+    u, v = uv_log_uniform(20000, 0.5 * duv, 0.45 * nxy / 2 * duv, seed=9)
+    re, im, w = _obs(20000, seed=10)
+    profiles = [1e10 * np.exp(-0.5 * ((R - (0.2 + 0.05 * k) * arcsec) / (0.05 * arcsec)) ** 2) for k in range(8)]
+
+    def run(k):
+        return g.double.chi2Profile(profiles[k], Rmin, dR, nxy, dxy, u, v, re, im, w, inc=0.1 * k, PA=0.2 * k)
+    seq = [run(k) for k in range(8)]
+    with ThreadPoolExecutor(max_workers=4) as ex:
+        par = list(ex.map(run, range(8)))
+    assert par == seq  # the same launches in the same order per call: bit-identical
