@@ -325,6 +325,72 @@ __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, 
 // the reference's flat-index semantics of the row-major N x C spectrum
 // (:774-780): a corner past the last column continues on the next row.
 // Returns false (and sets err bits) when a corner is outside the spectrum.
+// The same for the real spectrum of a swept profile (corners y real, z real):
+// amp * exp(i sign_u arg z) = (amp * sign(z), 0).  Corners come from the real
+// cell records, or from the window's real parts when it exceeds the record
+// capacity.  Writes the real result to *out.
+template <typename T>
+__device__ __forceinline__ bool interp_cell_real(const typename Launch<T>::VisArgs& a, const Window& w, int fu,
+                                                 int fv, T q, T t, T* out, unsigned* err) {
+    const int C = a.ncol;
+    int r0 = fv, c0 = fu;
+    while (c0 >= C) {  // flat-index continuation on the next row; fu < 4N bounds the loop
+        c0 -= C;
+        r0 += 1;
+    }
+    const bool wrap = (c0 + 1 == C);
+    const int r_last = wrap ? r0 + 2 : r0 + 1;
+    if (r0 < 0 || r_last >= a.nrow) {
+        *err |= ERR_UV_OUTSIDE;
+        return false;
+    }
+    const int qq = r0 - w.r0;
+    T yr[4];
+    if ((long long)w.K * w.W <= a.quad_cap) {
+        const bool inside = wrap ? (w.K == C && qq >= 0 && qq < w.W - 2) : (c0 < w.K - 1 && qq >= 0 && qq < w.W - 1);
+        if (!inside) {
+            *err |= ERR_WINDOW;
+            return false;
+        }
+        const T* rec = a.quads + ((long long)c0 * w.W + qq) * 4;
+        if constexpr (sizeof(T) == 4) {
+            const float4 p0 = __ldg(reinterpret_cast<const float4*>(rec));
+            yr[0] = p0.x;
+            yr[1] = p0.y;
+            yr[2] = p0.z;
+            yr[3] = p0.w;
+        } else {
+            const double2 p0 = __ldg(reinterpret_cast<const double2*>(rec));
+            const double2 p1 = __ldg(reinterpret_cast<const double2*>(rec) + 1);
+            yr[0] = p0.x;
+            yr[1] = p0.y;
+            yr[2] = p1.x;
+            yr[3] = p1.y;
+        }
+    } else {
+        const int rr[4] = {r0, r0 + 1, r_last, wrap ? r0 + 1 : r0};
+        const int cc[4] = {c0, c0, wrap ? 0 : c0 + 1, wrap ? 0 : c0 + 1};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int qc = rr[c] - w.r0;
+            if (cc[c] >= w.K || qc < 0 || qc >= w.W) {
+                *err |= ERR_WINDOW;
+                return false;
+            }
+            yr[c] = __ldg(&a.spec[(long long)qc * a.s_row + (long long)cc[c] * a.s_col]).x;
+        }
+    }
+    const T d1 = (yr[0] + yr[2]) - (yr[1] + yr[3]);
+    const T zr = t * (q * d1) + (t * (yr[1] - yr[0]) + q * (yr[3] - yr[0])) + yr[0];
+    const T m0 = fabs(yr[0]), m1 = fabs(yr[1]), m2 = fabs(yr[2]), m3 = fabs(yr[3]);
+    T amp = m0;
+    amp += (m3 - m0) * q;
+    amp += (m1 - m0) * t;
+    amp += (m0 - m1 + m2 - m3) * t * q;
+    *out = zr < (T)0 ? -amp : amp;
+    return true;
+}
+
 template <typename T>
 __device__ __forceinline__ bool interp_cell(const typename Launch<T>::VisArgs& a, const Window& w, int fu, int fv,
                                             T q, T t, T sign_u, C2<T>* out, unsigned* err) {
@@ -344,39 +410,6 @@ __device__ __forceinline__ bool interp_cell(const typename Launch<T>::VisArgs& a
     CT y[4];
     T am[4];
     const int qq = r0 - w.r0;
-    if (a.real_quads && (long long)w.K * w.W <= a.quad_cap) {
-        // real spectrum: z is real, so amp * exp(i sign_u arg z) = (amp sign(z), 0)
-        const bool inside = wrap ? (w.K == C && qq >= 0 && qq < w.W - 2) : (c0 < w.K - 1 && qq >= 0 && qq < w.W - 1);
-        if (!inside) {
-            *err |= ERR_WINDOW;
-            return false;
-        }
-        const T* rec = a.quads + ((long long)c0 * w.W + qq) * 4;
-        T yr[4];
-        if constexpr (sizeof(T) == 4) {
-            const float4 p0 = __ldg(reinterpret_cast<const float4*>(rec));
-            yr[0] = p0.x;
-            yr[1] = p0.y;
-            yr[2] = p0.z;
-            yr[3] = p0.w;
-        } else {
-            const double2 p0 = __ldg(reinterpret_cast<const double2*>(rec));
-            const double2 p1 = __ldg(reinterpret_cast<const double2*>(rec) + 1);
-            yr[0] = p0.x;
-            yr[1] = p0.y;
-            yr[2] = p1.x;
-            yr[3] = p1.y;
-        }
-        const T d1 = (yr[0] + yr[2]) - (yr[1] + yr[3]);
-        const T zr = t * (q * d1) + (t * (yr[1] - yr[0]) + q * (yr[3] - yr[0])) + yr[0];
-        const T m0 = fabs(yr[0]), m1 = fabs(yr[1]), m2 = fabs(yr[2]), m3 = fabs(yr[3]);
-        T amp = m0;
-        amp += (m3 - m0) * q;
-        amp += (m1 - m0) * t;
-        amp += (m0 - m1 + m2 - m3) * t * q;
-        *out = CT{zr < (T)0 ? -amp : amp, (T)0};
-        return true;
-    }
     if (a.quads && (long long)w.K * w.W <= a.quad_cap) {
         // one cell record: corners and moduli in 3 (FP32) or 6 (FP64) 16-byte loads
         const bool inside = wrap ? (w.K == C && qq >= 0 && qq < w.W - 2) : (c0 < w.K - 1 && qq >= 0 && qq < w.W - 1);
@@ -451,7 +484,7 @@ __device__ __forceinline__ bool interp_cell(const typename Launch<T>::VisArgs& a
 }
 
 // One visibility: rotation, index, interpolation and phase shift.
-template <typename T>
+template <typename T, bool REALQ>
 __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a, const Window& w, T u_in, T v_in,
                                            unsigned* e) {
     using CT = C2<T>;
@@ -475,7 +508,18 @@ __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a,
             return out;
         }
         const double fu = floor(indu), fv = floor(indv);
-        if (interp_cell<T>(a, w, (int)fu, (int)fv, (T)(indu - fu), (T)(indv - fv), (T)sign_u, &out, e) && a.phase) {
+        if constexpr (REALQ) {
+            T amp;
+            if (interp_cell_real<T>(a, w, (int)fu, (int)fv, (T)(indu - fu), (T)(indv - fv), &amp, e)) {
+                out = CT{amp, (T)0};
+                if (a.phase) {
+                    double sn, cs;
+                    sincos2pi_tab(ur * a.dra + vr * a.ddec, a.phase_tab, &sn, &cs);
+                    out = CT{amp * (T)cs, amp * (T)sn};
+                }
+            }
+        } else if (interp_cell<T>(a, w, (int)fu, (int)fv, (T)(indu - fu), (T)(indv - fv), (T)sign_u, &out, e) &&
+                   a.phase) {
             double sn, cs;
             sincos2pi_tab(ur * a.dra + vr * a.ddec, a.phase_tab, &sn, &cs);
             out = cmul(out, CT{(T)cs, (T)sn});
@@ -506,7 +550,15 @@ __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a,
         float q, t;
         df_floor(indu, &fu, &q);
         df_floor(indv, &fv, &t);
-        if (interp_cell<T>(a, w, fu, fv, (T)q, (T)t, (T)sign_u, &out, e) && a.phase) {
+        bool ok;
+        if constexpr (REALQ) {
+            T amp;
+            ok = interp_cell_real<T>(a, w, fu, fv, (T)q, (T)t, &amp, e);
+            if (ok) out = CT{amp, (T)0};
+        } else {
+            ok = interp_cell<T>(a, w, fu, fv, (T)q, (T)t, (T)sign_u, &out, e);
+        }
+        if (ok && a.phase) {
             const DF ph = df_add(df_mul(ur, a.dra_df), df_mul(vr, a.ddec_df));
             float n;
             if (fabsf(ph.hi) < 4194304.f) rint_i(ph.hi, &n);
@@ -514,7 +566,8 @@ __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a,
             const float f = __fadd_rn(__fsub_rn(ph.hi, n), ph.lo);  // cycles, |f| <= 1/2 + tiny
             float sn, cs;
             sincos2pi_f32(f, &sn, &cs);
-            out = cmul(out, CT{(T)cs, (T)sn});
+            if constexpr (REALQ) out = CT{out.x * (T)cs, out.x * (T)sn};
+            else out = cmul(out, CT{(T)cs, (T)sn});
         }
     }
     return out;
@@ -522,7 +575,7 @@ __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a,
 
 // Grid-stride over the visibilities, two independent points per iteration so
 // their load -> gather chains overlap.
-template <typename T, bool CHI2, bool VISOUT>
+template <typename T, bool CHI2, bool VISOUT, bool REALQ>
 __global__ void __launch_bounds__(256) vis_kernel(typename Launch<T>::VisArgs a) {
     using CT = C2<T>;
     __shared__ double sh[32];
@@ -548,8 +601,8 @@ __global__ void __launch_bounds__(256) vis_kernel(typename Launch<T>::VisArgs a)
             }
         }
         unsigned e0 = 0u, e1 = 0u;
-        const CT o0 = vis_point<T>(a, w, u0, v0, &e0);
-        const CT o1 = has1 ? vis_point<T>(a, w, u1, v1, &e1) : CT{(T)0, (T)0};
+        const CT o0 = vis_point<T, REALQ>(a, w, u0, v0, &e0);
+        const CT o1 = has1 ? vis_point<T, REALQ>(a, w, u1, v1, &e1) : CT{(T)0, (T)0};
         if (e0 | e1) {
             err |= e0 | e1;
             if (err_idx < 0) err_idx = e0 ? i0 : i1;
@@ -884,10 +937,17 @@ template <typename T> cudaError_t Launch<T>::vis(const VisArgs& args, cudaStream
     a.finalize();
     const int blocks = vis_grid(a.nd);
     const bool chi2 = a.partials != nullptr, vo = a.vis_out != nullptr;
-    if (chi2 && vo) vis_kernel<T, true, true><<<blocks, 256, 0, s>>>(a);
-    else if (chi2) vis_kernel<T, true, false><<<blocks, 256, 0, s>>>(a);
-    else if (vo) vis_kernel<T, false, true><<<blocks, 256, 0, s>>>(a);
-    else return cudaErrorInvalidValue;
+    // real_quads: the spectrum of a swept profile, interpolated as a real spectrum
+    if (!(chi2 || vo)) return cudaErrorInvalidValue;
+    if (a.real_quads && a.quads) {
+        if (chi2 && vo) vis_kernel<T, true, true, true><<<blocks, 256, 0, s>>>(a);
+        else if (chi2) vis_kernel<T, true, false, true><<<blocks, 256, 0, s>>>(a);
+        else vis_kernel<T, false, true, true><<<blocks, 256, 0, s>>>(a);
+    } else {
+        if (chi2 && vo) vis_kernel<T, true, true, false><<<blocks, 256, 0, s>>>(a);
+        else if (chi2) vis_kernel<T, true, false, false><<<blocks, 256, 0, s>>>(a);
+        else vis_kernel<T, false, true, false><<<blocks, 256, 0, s>>>(a);
+    }
     return cudaGetLastError();
 }
 
