@@ -55,7 +55,9 @@ void set_error_message(const std::string& msg);  // gb_api.cu
 namespace {
 
 constexpr int kVisThreads = 256;
-constexpr int kVisWarps = kVisThreads / 32;
+// threads of a vis block with PTS visibilities per thread: spans of 512 or
+// 1024 visibilities, so that no block straddles two sets (kSetAlign)
+constexpr int vis_threads(int pts) { return pts >= 8 ? 1024 / pts : kVisThreads; }
 constexpr int kRowsPerCta = 16;  // folded image rows (up to two box rows each) per CTA in the row adjoint
 constexpr int kGRec = 12;       // floats per gradient cell record
 constexpr int kTmaCols = 100;   // column-pass shape code: E + kTmaCols selects the TMA-fed variant
@@ -267,6 +269,7 @@ __global__ void quadT_real_kernel(Geo g, const float* __restrict__ cgrad4, const
         take(k - 1, q, 3);
         const size_t el = (size_t)b * ncell + (size_t)k * g.W + q;
         const float y = wr[el];
+        ga *= 2.f;  // the vis pass records halves of dchi2/dA
         float gy = y < 0.f ? -ga : (y > 0.f ? ga : 0.f);
         const int row = g.r0 + q;
         if (((row + k + g.N / 2) & 1)) gy = -gy;
@@ -500,12 +503,7 @@ __device__ __forceinline__ void apply_phase_point(const ModelConst& m, float u, 
     p.ps = 0.f;
     if (m.phase) {
         // u'dRA' + v'dDec' = u dRA + v dDec (both pairs rotated by PA)
-        const DF ph = df_dot2(u, m.dra, v, m.ddec);
-        float n;
-        if (fabsf(ph.hi) < 4194304.f) rint_i(ph.hi, &n);
-        else n = rintf(ph.hi);
-        const float f = __fadd_rn(__fsub_rn(ph.hi, n), ph.lo);
-        sincos2pi_f32(f, &p.ps, &p.pc);
+        sincos2pi_df(df_dot2(u, m.dra, v, m.ddec), &p.ps, &p.pc);
         U = make_float2(U.x * p.pc - U.y * p.ps, U.x * p.ps + U.y * p.pc);
     }
     p.V = U;
@@ -548,38 +546,87 @@ __device__ __forceinline__ void eval_point(const Geo& g, const ModelConst& m, co
     apply_phase_point(m, u, v, make_float2(A * cph, A * sph), p);
 }
 
-// The spectrum of a swept profile is real (the image is even in x and y):
-// the window holds one real per element, z is real and
-// amp * exp(i sign_u arg z) = (amp * sign(z), 0).  p.y[c].x are the corners,
-// p.am[c] their moduli, p.zr = z, p.rn = sign(z).
-__device__ __forceinline__ void eval_point_real(const Geo& g, const ModelConst& m, const float* __restrict__ wr_b,
-                                                float u, float v, PointEval& p) {
-    int c0c, qqc;
-    locate_point(g, m, u, v, p, &c0c, &qqc);
-    const float* e0 = wr_b + (size_t)c0c * g.W + qqc;
-    const float y0 = __ldg(e0), y1 = __ldg(e0 + 1), y2 = __ldg(e0 + g.W + 1), y3 = __ldg(e0 + g.W);
-    p.y[0].x = y0;
-    p.y[1].x = y1;
-    p.y[2].x = y2;
-    p.y[3].x = y3;
-    p.am[0] = fabsf(y0);
-    p.am[1] = fabsf(y1);
-    p.am[2] = fabsf(y2);
-    p.am[3] = fabsf(y3);
-    const float t = p.t, q = p.q;
-    const float d1 = (y0 + y2) - (y1 + y3);
-    p.zr = t * (q * d1) + (t * (y1 - y0) + q * (y3 - y0)) + y0;
-    float A = p.am[0];
-    A += (p.am[3] - p.am[0]) * q;
-    A += (p.am[1] - p.am[0]) * t;
-    A += (p.am[0] - p.am[1] + p.am[2] - p.am[3]) * t * q;
-    p.A = A;
-    p.rn = p.zr < 0.f ? -1.f : 1.f;
-    apply_phase_point(m, u, v, make_float2(A * p.rn, 0.f), p);
-}
-
 // Accumulators per model and block: chi2, dPA, dRA, dDec
 constexpr int kAcc = 4;
+
+// One (visibility, model) of a real window (swept profiles, origin 'upper',
+// every term evaluated, no branch: padding points have w = 0 and (u, v) = 0,
+// so they add zero everywhere).  V = A sign(z) exp(2 pi i (u dRA + v dDec))
+// with A the bilinear modulus and z the bilinear signed value of the cell's
+// corners.  Returns the chi2 term.  With GRAD: hA = (dchi2/dA) / 2 for the
+// cell's corner moments, and acc[1..3] += halves of dchi2/dPA and of
+// dchi2/d(dRA, dDec) / (2 pi); kReal_scale restores the factors once per model.
+struct RealPoint {
+    float hA, t, q;
+    int cell;
+};
+template <bool GRAD>
+__device__ __forceinline__ float real_point(const Geo& g, const ModelConst& m, const float* __restrict__ wr_b,
+                                            float u, float v, float re, float im, float w, float* acc,
+                                            RealPoint& e, unsigned& err) {
+    // rotated coordinates in grid units: a = u'/duv, c = v'/duv
+    const DF a = df_dot2(u, m.cu, -v, m.sv);
+    const DF cv = df_dot2(u, m.sv, v, m.cu);
+    // u' < 0 reads the Hermitian point (-u', -v'); a real spectrum is unchanged by it
+    const bool neg = a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f);
+    const DF indu = neg ? df_neg(a) : a;
+    const float cs = neg ? -cv.hi : cv.hi, cl = neg ? -cv.lo : cv.lo;
+    const float vh = __fadd_rn(g.half_nrow, cs);  // N/2 + c: Fast2Sum (|c| < N/2)
+    const DF indv{vh, __fadd_rn(__fsub_rn(cs, __fsub_rn(vh, g.half_nrow)), cl)};
+    int fu, fv;
+    float q, t;
+    df_floor(indu, &fu, &q);
+    df_floor(indv, &fv, &t);
+    const int qq = fv - g.r0;
+    const int c0 = min(max(fu, 0), g.K - 2), q0 = min(max(qq, 0), g.W - 2);
+    if (c0 != fu || q0 != qq) err |= ERR_WINDOW;
+    e.cell = c0 * g.W + q0;
+    e.t = t;
+    e.q = q;
+    // corners (k, q), (k, q+1), (k+1, q+1), (k+1, q) of the column-major window
+    const float* e0 = wr_b + e.cell;
+    const float y0 = __ldg(e0), y1 = __ldg(e0 + 1), y2 = __ldg(e0 + g.W + 1), y3 = __ldg(e0 + g.W);
+    const float a0 = fabsf(y0), a1 = fabsf(y1), a2 = fabsf(y2), a3 = fabsf(y3);
+    const float D = (a0 - a1) + (a2 - a3);
+    const float dAq = fmaf(t, D, a3 - a0);  // dA/dq
+    const float A = fmaf(q, dAq, fmaf(t, a1 - a0, a0));
+    const float z = fmaf(q, fmaf(t, (y0 - y1) + (y2 - y3), y3 - y0), fmaf(t, y1 - y0, y0));
+    const float As = z < 0.f ? -A : A;
+    float ps, pc;
+    sincos2pi_df(df_dot2(u, m.dra, v, m.ddec), &ps, &pc);
+    const float vx = As * pc, vy = As * ps;
+    const float dr = vx - re, di = vy - im;
+    const float hx = w * dr, hy = w * di;  // (dchi2/dV) / 2
+    if constexpr (GRAD) {
+        const float gAs = fmaf(hx, pc, hy * ps);
+        e.hA = z < 0.f ? -gAs : gAs;
+        // phase 2 pi (u dRA + v dDec): (dchi2/dphi) / 2 = Im(conj(V) h)
+        const float dphi = fmaf(hy, vx, -hx * vy);
+        acc[2] = fmaf(dphi, u, acc[2]);
+        acc[3] = fmaf(dphi, v, acc[3]);
+        // position: q = |a|, t = N/2 + sign(a) c; da/dPA = -c, dc/dPA = a
+        const float dAt = fmaf(q, D, a1 - a0);  // dA/dt
+        acc[1] = fmaf(e.hA, fmaf(dAt, indu.hi, -dAq * cs), acc[1]);
+    }
+    return fmaf(dr, hx, di * hy);
+}
+
+// lane l of a warp ends with the warp's sum of a[(l >> 3) & 3]: one exchange
+// of two values, one of one value, then three single-value halvings
+__device__ __forceinline__ float warp_sum4(const float* a, int lane) {
+    const unsigned full = 0xffffffffu;
+    const bool h16 = lane & 16, h8 = lane & 8;
+    float k0 = h16 ? a[2] : a[0], k1 = h16 ? a[3] : a[1];
+    const float s0 = h16 ? a[0] : a[2], s1 = h16 ? a[1] : a[3];
+    k0 += __shfl_xor_sync(full, s0, 16);
+    k1 += __shfl_xor_sync(full, s1, 16);
+    float k = h8 ? k1 : k0;
+    k += __shfl_xor_sync(full, h8 ? k0 : k1, 8);
+    k += __shfl_xor_sync(full, k, 4);
+    k += __shfl_xor_sync(full, k, 2);
+    k += __shfl_xor_sync(full, k, 1);
+    return k;
+}
 
 // PTS consecutive entries of a float array, one vector load when aligned and in range
 template <int PTS>
@@ -637,9 +684,9 @@ template <bool REAL> __device__ __forceinline__ void emit_run(float* __restrict_
     else emit_cell(cg, cell, M);
 }
 
-// Grid: x = blocks of kVisThreads * PTS visibilities, y = groups of Bg
-// models.  The hardware issues the x blocks of one group before the next, so
-// the windows (and gradient records) of about Bg models are live in L2 at a time.
+// Grid: x = blocks of NT * PTS visibilities, y = groups of Bg models.  The
+// hardware issues the x blocks of one group before the next, so the windows
+// (and gradient records) of about Bg models are live in L2 at a time.
 //
 // Thread t of a block owns the PTS consecutive visibilities t*PTS .. t*PTS+PTS-1
 // of the block's span (vector loads; consecutive in the Morton order, so they
@@ -650,17 +697,18 @@ template <bool REAL> __device__ __forceinline__ void emit_run(float* __restrict_
 // lane; the last runs then go through one warp-segmented reduction (shuffles)
 // and one lane per run of equal cells adds it.
 // REAL: the window is real (swept profiles): one float per element, one
-// gradient component (dchi2/dA) per corner, 4-float cell records.
-template <bool GRAD, int PTS, bool REAL>
-__global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, int Bg, int nd, const float* __restrict__ u,
-                                                                const float* __restrict__ v,
-                                                                const float* __restrict__ re,
-                                                                const float* __restrict__ im,
-                                                                const float* __restrict__ w,
-                                                                const ModelConst* __restrict__ mc,
-                                                                const void* __restrict__ wel_any,
-                                                                float* __restrict__ cgrad, double* __restrict__ partials,
-                                                                DevState* st) {
+// gradient component (dchi2/dA) per corner, 4-float cell records, and the
+// point evaluation of real_point (halved gradients, restored per model).
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+
+template <bool GRAD, int PTS, bool REAL, int NT>
+__global__ void __launch_bounds__(NT) vis_batch_kernel(Geo g, int B, int Bg, int nd, const float* __restrict__ u,
+                                                       const float* __restrict__ v, const float* __restrict__ re,
+                                                       const float* __restrict__ im, const float* __restrict__ w,
+                                                       const ModelConst* __restrict__ mc,
+                                                       const void* __restrict__ wel_any, float* __restrict__ cgrad,
+                                                       double* __restrict__ partials, DevState* st) {
+    constexpr int NW = NT / 32;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int b0 = blockIdx.y * Bg;
     const int nb = min(Bg, B - b0);
@@ -669,7 +717,7 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
     // and no barrier between models
     float* wacc = reinterpret_cast<float*>(smc + Bg);
     // each thread's first run of equal cells (moments), read by the previous lane
-    float* fst_all = wacc + Bg * kAcc * kVisWarps;
+    float* fst_all = wacc + Bg * kAcc * NW;
     constexpr int NR = REAL ? 4 : 12;              // floats of a run's moments
     constexpr int FS = REAL ? 5 : kFirstStride;   // odd slot stride: no bank conflicts
     float* fst = fst_all + threadIdx.x * FS;
@@ -679,7 +727,7 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
     for (int i = threadIdx.x; i < nb; i += blockDim.x) smc[i] = mc[b0 + i];
     // this thread's points
     float pu[PTS], pv[PTS], pre[PTS], pim[PTS], pw[PTS];
-    const long long i0 = ((long long)blockIdx.x * kVisThreads + threadIdx.x) * PTS;
+    const long long i0 = ((long long)blockIdx.x * NT + threadIdx.x) * PTS;
     load_pts<PTS>(u, i0, nd, pu);
     load_pts<PTS>(v, i0, nd, pv);
     load_pts<PTS>(re, i0, nd, pre);
@@ -700,13 +748,36 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
         for (int cc = 0; cc < NR; ++cc) run[cc] = 0.f;
 #pragma unroll
         for (int j = 0; j < PTS; ++j) {
+            if constexpr (REAL) {
+                RealPoint e;
+                acc[0] += real_point<GRAD>(g, m, welr + (size_t)b * ncell, pu[j], pv[j], pre[j], pim[j], pw[j], acc,
+                                           e, err);
+                if constexpr (GRAD) {
+                    const float mom[4] = {1.f, e.t, e.q, e.t * e.q};
+                    const bool same = e.cell == cur;
+                    if (!same) {
+                        if (cur >= 0) {
+                            if (fcell < 0) {
+                                fcell = cur;
+#pragma unroll
+                                for (int cc = 0; cc < NR; ++cc) fst[cc] = run[cc];
+                            } else {
+                                emit_run<REAL>(cg, cur, run);  // begins and ends inside this thread
+                            }
+                        }
+                        cur = e.cell;
+                    }
+#pragma unroll
+                    for (int mm = 0; mm < 4; ++mm) run[mm] = fmaf(e.hA, mom[mm], same ? run[mm] : 0.f);
+                }
+                continue;
+            } else {
             const bool live = pw[j] != 0.f;  // w = 0: padding (or a zero-weight visibility)
             PointEval p;
             p.cell = -1;
             p.V = make_float2(0.f, 0.f);
             if (live) {
-                if constexpr (REAL) eval_point_real(g, m, welr + (size_t)b * ncell, pu[j], pv[j], p);
-                else eval_point(g, m, wel + (size_t)b * ncell, pu[j], pv[j], p);
+                eval_point(g, m, wel + (size_t)b * ncell, pu[j], pv[j], p);
                 err |= p.err;
             }
             const float dr = p.V.x - pre[j], di = p.V.y - pim[j];
@@ -719,48 +790,37 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
                 acc[2] += dphi * 6.28318530717958647692f * pu[j];
                 acc[3] += dphi * 6.28318530717958647692f * pv[j];
                 const float t = p.t, q = p.q;
-                float gv[NR], dAq, dAt, gq, gt;
-                if constexpr (REAL) {
-                    // U = (A s, 0), s = sign(z): only the modulus path carries a gradient
-                    const float gA = (gx * p.pc + gy * p.ps) * p.rn;
-                    gv[0] = gA;
-                    dAq = (p.am[3] - p.am[0]) + t * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
-                    dAt = (p.am[1] - p.am[0]) + q * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
-                    gq = gA * dAq;
-                    gt = gA * dAt;
-                } else {
-                    // G_U = G conj(P)
-                    const float gux = gx * p.pc + gy * p.ps, guy = -gx * p.ps + gy * p.pc;
-                    // U = A * (zr, su zi) / |z|
-                    const float ex = p.zr * p.rn, ey = p.zi * p.rn;  // e = z/|z|
-                    const float gA = gux * ex + guy * (p.su * ey);
-                    // gradient w.r.t. e (undo the conjugation for u < 0)
-                    const float gex = p.A * gux, gey = p.su * p.A * guy;
-                    const float dot = ex * gex + ey * gey;
-                    const float gzx = (gex - ex * dot) * p.rn, gzy = (gey - ey * dot) * p.rn;
-                    // position: q = |a|, t = N/2 + vo su c with a = u'/duv, c = v'/duv;
-                    // da/dPA = -c, dc/dPA = a
-                    const float dzqx = (p.y[3].x - p.y[0].x) + t * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
-                    const float dzqy = (p.y[3].y - p.y[0].y) + t * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
-                    const float dztx = (p.y[1].x - p.y[0].x) + q * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
-                    const float dzty = (p.y[1].y - p.y[0].y) + q * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
-                    dAq = (p.am[3] - p.am[0]) + t * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
-                    dAt = (p.am[1] - p.am[0]) + q * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
-                    gq = gzx * dzqx + gzy * dzqy + gA * dAq;
-                    gt = gzx * dztx + gzy * dzty + gA * dAt;
-                    gv[0] = gzx;
-                    gv[1] = gzy;
-                    gv[2] = gA;
-                }
+                float gv[NR];
+                // G_U = G conj(P)
+                const float gux = gx * p.pc + gy * p.ps, guy = -gx * p.ps + gy * p.pc;
+                // U = A * (zr, su zi) / |z|
+                const float ex = p.zr * p.rn, ey = p.zi * p.rn;  // e = z/|z|
+                const float gA = gux * ex + guy * (p.su * ey);
+                // gradient w.r.t. e (undo the conjugation for u < 0)
+                const float gex = p.A * gux, gey = p.su * p.A * guy;
+                const float dot = ex * gex + ey * gey;
+                const float gzx = (gex - ex * dot) * p.rn, gzy = (gey - ey * dot) * p.rn;
+                // position: q = |a|, t = N/2 + vo su c with a = u'/duv, c = v'/duv;
+                // da/dPA = -c, dc/dPA = a
+                const float dzqx = (p.y[3].x - p.y[0].x) + t * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
+                const float dzqy = (p.y[3].y - p.y[0].y) + t * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
+                const float dztx = (p.y[1].x - p.y[0].x) + q * ((p.y[0].x - p.y[1].x) + (p.y[2].x - p.y[3].x));
+                const float dzty = (p.y[1].y - p.y[0].y) + q * ((p.y[0].y - p.y[1].y) + (p.y[2].y - p.y[3].y));
+                const float dAq = (p.am[3] - p.am[0]) + t * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
+                const float dAt = (p.am[1] - p.am[0]) + q * ((p.am[0] - p.am[1]) + (p.am[2] - p.am[3]));
+                const float gq = gzx * dzqx + gzy * dzqy + gA * dAq;
+                const float gt = gzx * dztx + gzy * dzty + gA * dAt;
+                gv[0] = gzx;
+                gv[1] = gzy;
+                gv[2] = gA;
                 acc[1] += gq * (p.su * (-p.vr)) + gt * (g.vo * p.su * p.ur);
                 // runs of equal cells within the thread, summed as moments in registers
-                constexpr int NC = NR / 4;  // gradient components per corner
                 const float mom[4] = {1.f, t, q, t * q};
                 if (p.cell == cur) {
 #pragma unroll
                     for (int mm = 0; mm < 4; ++mm)
 #pragma unroll
-                        for (int i = 0; i < NC; ++i) run[NC * mm + i] = fmaf(gv[i], mom[mm], run[NC * mm + i]);
+                        for (int i = 0; i < 3; ++i) run[3 * mm + i] = fmaf(gv[i], mom[mm], run[3 * mm + i]);
                 } else {
                     if (cur >= 0) {
                         if (fcell < 0) {
@@ -775,8 +835,9 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
 #pragma unroll
                     for (int mm = 0; mm < 4; ++mm)
 #pragma unroll
-                        for (int i = 0; i < NC; ++i) run[NC * mm + i] = gv[i] * mom[mm];
+                        for (int i = 0; i < 3; ++i) run[3 * mm + i] = gv[i] * mom[mm];
                 }
+            }
             }
         }
         if (GRAD) {
@@ -813,24 +874,27 @@ __global__ void __launch_bounds__(kVisThreads) vis_batch_kernel(Geo g, int B, in
             }
             if (cur >= 0 && ((heads >> lane) & 1u)) emit_run<REAL>(cg, cur, run);
             __syncwarp();  // the slots are rewritten for the next model
-        }
-        // warp sums of this model's accumulators
-#pragma unroll
-        for (int a = 0; a < (GRAD ? kAcc : 1); ++a) {
-            float x = acc[a];
+            // warp sums of the four accumulators: lanes 0, 8, 16, 24 hold them
+            const float x = warp_sum4(acc, lane);
+            if ((lane & 7) == 0) wacc[(bl * kAcc + (lane >> 3)) * NW + wid] = x;
+        } else {
+            float x = acc[0];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            if (lane == 0) wacc[(bl * kAcc + a) * kVisWarps + wid] = x;
+            if (lane == 0) wacc[(bl * kAcc) * NW + wid] = x;
         }
     }
     if (err) atomicOr(&st->err, err);
     __syncthreads();
+    // real_point accumulates halves of dchi2/dPA and of dchi2/d(dRA, dDec) / (2 pi)
     double* dst = partials + ((size_t)blockIdx.x * B + b0) * kAcc;
     for (int i = threadIdx.x; i < nb * kAcc; i += blockDim.x) {
+        const int a = i % kAcc;
         double s = 0.0;
-        if (GRAD || (i % kAcc) == 0) {
-            for (int q = 0; q < kVisWarps; ++q) s += (double)wacc[i * kVisWarps + q];
+        if (GRAD || a == 0) {
+            for (int q = 0; q < NW; ++q) s += (double)wacc[i * NW + q];
         }
+        if (REAL && a > 0) s *= (a == 1 ? 2.0 : 2.0 * kTwoPi);
         dst[i] = s;
     }
 }
@@ -1901,23 +1965,27 @@ static void batch_run(const BatchCall& call) {
             BCK(cudaGetLastError());
         };
         auto vis = [&](int pts) {
-            const int vb = (int)((d->nd_pad + (long long)kVisThreads * pts - 1) / ((long long)kVisThreads * pts));
-            const size_t vsm = sizeof(ModelConst) * Bg + sizeof(float) * Bg * kAcc * kVisWarps +
-                               (grad ? sizeof(float) * kVisThreads * (real ? 5 : kFirstStride) : 0);
+            const int nt = vis_threads(pts);
+            const int vb = (int)((d->nd_pad + (long long)nt * pts - 1) / ((long long)nt * pts));
+            const size_t vsm = sizeof(ModelConst) * Bg + sizeof(float) * Bg * kAcc * (nt / 32) +
+                               (grad ? sizeof(float) * nt * (real ? 5 : kFirstStride) : 0);
             const dim3 grid(vb, ngroups);
 #define GBB_VIS(G_, P_, R_)                                                                                    \
     do {                                                                                                       \
-        BCK((cudaError_t)smem_attr((const void*)vis_batch_kernel<G_, P_, R_>, vsm));                           \
-        vis_batch_kernel<G_, P_, R_><<<grid, kVisThreads, vsm, s>>>(g, B, Bg, d->nd_pad, d->u, d->v, d->re,   \
-                                                                   d->im, d->w, mc, (const void*)wel, cgrad,  \
-                                                                   partials, st);                             \
+        constexpr int NT_ = vis_threads(P_);                                                                   \
+        BCK((cudaError_t)smem_attr((const void*)vis_batch_kernel<G_, P_, R_, NT_>, vsm));                      \
+        vis_batch_kernel<G_, P_, R_, NT_><<<grid, NT_, vsm, s>>>(g, B, Bg, d->nd_pad, d->u, d->v, d->re,      \
+                                                                d->im, d->w, mc, (const void*)wel, cgrad,     \
+                                                                partials, st);                                \
     } while (0)
             if (real) {
                 if (grad) {
                     if (pts == 2) GBB_VIS(true, 2, true);
+                    else if (pts == 8) GBB_VIS(true, 8, true);
                     else GBB_VIS(true, 4, true);
                 } else {
                     if (pts == 2) GBB_VIS(false, 2, true);
+                    else if (pts == 8) GBB_VIS(false, 8, true);
                     else GBB_VIS(false, 4, true);
                 }
             } else {
@@ -1992,7 +2060,7 @@ static void batch_run(const BatchCall& call) {
             if (grad) zero_grads();
             vis(sh.pts);
             batch_finalize_kernel<<<dim3(B, grad ? kAcc : 1), 256, 0, s>>>(
-                B, d->nsets, d->set_pad_d, kVisThreads * sh.pts, partials, chi2, chi2_sets, gsum);
+                B, d->nsets, d->set_pad_d, vis_threads(sh.pts) * sh.pts, partials, chi2, chi2_sets, gsum);
             BCK(cudaGetLastError());
             if (!grad) return;
             // ---- adjoint ----
@@ -2028,7 +2096,8 @@ static void batch_run(const BatchCall& call) {
                 for (int e : fft_candidates(g.N)) col_shapes.push_back(e + kTmaCols);
             sh.e_rows = tu.best(fft_candidates(g.M), [&](int e) { sh.e_rows = e; run_all(); });
             sh.e_cols = tu.best(col_shapes, [&](int e) { sh.e_cols = e; run_all(); });
-            sh.pts = tu.best({2, 4}, [&](int p) { sh.pts = p; run_all(); });
+            sh.pts = tu.best(real ? std::vector<int>{2, 4, 8} : std::vector<int>{2, 4},
+                             [&](int p) { sh.pts = p; run_all(); });
             if (grad) {
                 sh.e_colsT = tu.best(fft_candidates(g.N), [&](int e) { sh.e_colsT = e; run_all(); });
                 sh.e_rowsT = tu.best(fft_candidates(g.M), [&](int e) { sh.e_rowsT = e; run_all(); });

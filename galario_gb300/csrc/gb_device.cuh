@@ -475,30 +475,26 @@ __device__ __forceinline__ DF df_add(DF a, DF b) {
     DF s = df_two_sum(a.hi, b.hi);
     return df_renorm(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
-// floor of x = hi + lo (|hi| < 2^22) as an integer and the fraction in [0, 1]
+// floor of x = hi + lo (|hi| < 2^22, |lo| at most a few ulps of hi) as an
+// integer and the fraction in [0, 1]: n = rint(hi) by the magic-number
+// method, hi - n is exact (Sterbenz), f = (hi - n) + lo lies in
+// [-1/2 - tiny, 1/2 + tiny], and a negative f moves to the integer below.
 __device__ __forceinline__ void df_floor(DF x, int* fl, float* frac) {
-    float f;
-    int n = floor_i(x.hi, &f);
-    float r = __fadd_rn(__fsub_rn(x.hi, f), x.lo);  // hi - floor(hi) is exact
-    if (r < 0.f) {
+    const float r = __fadd_rn(x.hi, kMagic);
+    float f = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(r, kMagic)), x.lo);
+    int n = __float_as_int(r) - kMagicBits;
+    if (f < 0.f) {
         n -= 1;
-        r = __fadd_rn(r, 1.f);
-    } else if (r >= 1.f) {
-        n += 1;
-        r = __fsub_rn(r, 1.f);
+        f = __fadd_rn(f, 1.f);
     }
     *fl = n;
-    *frac = r;
+    *frac = f;
 }
 
-// sin/cos(2 pi f) in FP32 for |f| <= 1/2 + tiny, without conversion
-// instructions: j = rint(4 f), d = f - j/4 (exact by Sterbenz), x = 2 pi d with
-// |x| <= pi/4, Taylor series to x^9 (sin) and x^8 (cos), truncation error
-// below 3e-8, then rotation by i^j.
-__device__ __forceinline__ void sincos2pi_f32(float f, float* s, float* c) {
-    float jf;
-    const int j = rint_i(4.f * f, &jf);
-    const float d = __fmaf_rn(jf, -0.25f, f);
+// sin/cos(2 pi (j/4 + d)) for |d| <= 1/8 + tiny: x = 2 pi d, |x| <= pi/4,
+// Taylor series to x^9 (sin) and x^8 (cos), truncation error below 3e-8, then
+// the rotation by i^j as a swap and two sign-bit flips.
+__device__ __forceinline__ void sincos2pi_quadrant(float d, unsigned j, float* s, float* c) {
     const float x = d * 6.28318530717958647692f;
     const float x2 = x * x;
     float sp = __fmaf_rn(x2, 2.7557319e-6f, -1.9841270e-4f);  // 1/9!, -1/7!
@@ -509,12 +505,32 @@ __device__ __forceinline__ void sincos2pi_f32(float f, float* s, float* c) {
     cp = __fmaf_rn(x2, cp, 4.1666667e-2f);                     // 1/4!
     cp = __fmaf_rn(x2, cp, -0.5f);
     const float cx = __fmaf_rn(x2, cp, 1.f);
-    switch (j & 3) {  // multiply by i^j
-        case 0: *s = sx; *c = cx; break;
-        case 1: *s = cx; *c = -sx; break;
-        case 2: *s = -sx; *c = -cx; break;
-        default: *s = -cx; *c = sx; break;
-    }
+    // i^j: (s, c) = (sx, cx), (cx, -sx), (-sx, -cx), (-cx, sx) for j = 0..3 (mod 4)
+    const bool odd = j & 1u;
+    const float so = odd ? cx : sx, co = odd ? sx : cx;
+    *s = __int_as_float(__float_as_int(so) ^ (int)((j & 2u) << 30));
+    *c = __int_as_float(__float_as_int(co) ^ (int)(((j + 1u) & 2u) << 30));
+}
+
+// sin/cos(2 pi f) in FP32 for |f| <= 1/2 + tiny, without conversion
+// instructions: j = rint(4 f), d = f - j/4 (exact by Sterbenz).
+__device__ __forceinline__ void sincos2pi_f32(float f, float* s, float* c) {
+    const float r = __fmaf_rn(f, 4.f, kMagic);
+    const float d = __fmaf_rn(__fsub_rn(r, kMagic), -0.25f, f);
+    sincos2pi_quadrant(d, (unsigned)(__float_as_int(r) - kMagicBits), s, c);
+}
+
+// sin/cos(2 pi (hi + lo)) for a double-float argument in turns (|hi| < 2^41,
+// |lo| at most a few ulps of hi), all in FP32: exact reductions by a whole
+// multiple of 2^20 turns (|h| <= 2^19 afterwards) and by quarter turns, each
+// with one magic-number rounding and one Sterbenz subtraction, then
+// d = (h - j/4) + lo and sincos2pi_quadrant.
+__device__ __forceinline__ void sincos2pi_df(DF ph, float* s, float* c) {
+    const float kb = __fsub_rn(__fmaf_rn(ph.hi, 0x1p-20f, kMagic), kMagic);
+    const float h = __fmaf_rn(kb, -0x1p20f, ph.hi);
+    const float r = __fmaf_rn(h, 4.f, kMagic);
+    const float d = __fadd_rn(__fmaf_rn(__fsub_rn(r, kMagic), -0.25f, h), ph.lo);
+    sincos2pi_quadrant(d, (unsigned)(__float_as_int(r) - kMagicBits), s, c);
 }
 
 

@@ -559,13 +559,9 @@ __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a,
             ok = interp_cell<T>(a, w, fu, fv, (T)q, (T)t, (T)sign_u, &out, e);
         }
         if (ok && a.phase) {
-            const DF ph = df_add(df_mul(ur, a.dra_df), df_mul(vr, a.ddec_df));
-            float n;
-            if (fabsf(ph.hi) < 4194304.f) rint_i(ph.hi, &n);
-            else n = rintf(ph.hi);  // |phase| >= 2^22 cycles: not reached for physical offsets
-            const float f = __fadd_rn(__fsub_rn(ph.hi, n), ph.lo);  // cycles, |f| <= 1/2 + tiny
+            const DF ph = df_add(df_mul(ur, a.dra_df), df_mul(vr, a.ddec_df));  // cycles
             float sn, cs;
-            sincos2pi_f32(f, &sn, &cs);
+            sincos2pi_df(ph, &sn, &cs);
             if constexpr (REALQ) out = CT{out.x * (T)cs, out.x * (T)sn};
             else out = cmul(out, CT{(T)cs, (T)sn});
         }
