@@ -117,6 +117,13 @@ struct Ctx {
     // (Re, Im, w) on it while the spectrum passes run on `stream`
     cudaStream_t side = nullptr;
     cudaEvent_t ev_side_start = nullptr, ev_obs = nullptr;
+    // overlapped host-pointer chi2Profile: (u, v) uploaded, then each chunk's observations
+    static constexpr int kMaxChunks = 4;
+    cudaEvent_t ev_uv = nullptr, ev_chunk[kMaxChunks] = {};
+    // odd chunks of the visibility pass run on vis2, so that one chunk's
+    // tail overlaps the next chunk's start
+    cudaStream_t vis2 = nullptr;
+    cudaEvent_t ev_win = nullptr, ev_vis2 = nullptr;
     DevBuf state, partials, img, prof, u, v, re, im, w, vis, zt, win, amp, quad, urot, vrot;
     double2* phase_tab = nullptr;  // table of the FP64 phase shift (PHASE_T + 1 entries)
     std::map<std::pair<int, int>, void*> tw;   // (N, sizeof(T)) -> table
@@ -147,6 +154,11 @@ struct Ctx {
         CK(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&ev_side_start, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&ev_obs, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ev_uv, cudaEventDisableTiming));
+        CK(cudaStreamCreateWithFlags(&vis2, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ev_win, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ev_vis2, cudaEventDisableTiming));
+        for (auto& e : ev_chunk) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         CK(cudaMallocHost(&host_state, sizeof(DevState)));
         // exp(2 pi i (j - T/2) / T), j in [0, T], evaluated in long double
         std::vector<double2> h(PHASE_T + 1);
@@ -307,6 +319,20 @@ ProfileGeom profile_geom(const T* I_host, int nr, double Rmin, double dR, double
 // ---------------------------------------------------------------------------
 // the pipeline, device side
 // ---------------------------------------------------------------------------
+// A host-pointer call whose uploads run on the side stream while the
+// spectrum passes run: the row pass writes every column (it does not wait
+// for the extent), the extent pass waits for ev_uv, and the visibility pass
+// runs in `nchunks` launches over consecutive ranges, chunk c after
+// ev_chunk[c] (its Re, Im, w uploaded), alternately on `stream` and `vis2`;
+// the chi2 reduction is finished by the last block of all chunks.
+struct Overlap {
+    cudaEvent_t ev_uv = nullptr;
+    int nchunks = 1;
+    const cudaEvent_t* ev_chunk = nullptr;
+};
+// chunk c of nd visibilities in n chunks: [chunk_begin(nd, n, c), chunk_begin(nd, n, c + 1))
+inline int chunk_begin(int nd, int n, int c) { return (int)((long long)nd * c / n); }
+
 template <typename T> struct Pipe {
     using CT = C2<T>;
     using L = Launch<T>;
@@ -317,7 +343,8 @@ template <typename T> struct Pipe {
                         double dR, double dxy, double inc, const ProfileGeom* pg, double v_origin, double dRA,
                         double dDec, double PA, int nd, const T* u, const T* v, const T* re, const T* im, const T* w,
                         CT* vis_out, bool chi2, double* chi2_out, DevState* st, bool have_extent,
-                        const std::function<void()>& before_vis = std::function<void()>()) {
+                        const std::function<void()>& before_vis = std::function<void()>(),
+                        const Overlap* ov = nullptr) {
         const int C = N / 2 + 1;
         const CT* tw = c.twiddles<T>(N);
         CT* zt = as<CT>(c.zt, (size_t)C * N);
@@ -325,8 +352,12 @@ template <typename T> struct Pipe {
         T* amp = as<T>(c.amp, (size_t)C * N);
         const long long qcap = std::min<long long>((long long)C * N, QUAD_CAP);
         T* quads = as<T>(c.quad, (size_t)qcap * QUAD_REC);
-        double* partials = as<double>(c.partials, (size_t)L::vis_grid(nd > 0 ? nd : 1));
-        if (!have_extent) timed(c, s, ST_EXTENT, [&] { CK(L::extent(u, v, nd, N, duv, st, s)); });
+        const int nchunks = (ov && nd > 0) ? ov->nchunks : 1;
+        size_t nparts = 0;
+        for (int k = 0; k < nchunks; ++k)
+            nparts += (size_t)L::vis_grid(std::max(1, chunk_begin(nd, nchunks, k + 1) - chunk_begin(nd, nchunks, k)));
+        double* partials = as<double>(c.partials, nparts);
+        if (!have_extent && !ov) timed(c, s, ST_EXTENT, [&] { CK(L::extent(u, v, nd, N, duv, st, s)); });
         int band0 = 0, band1 = N;
         const CT* stw_rows = c.stage_tw<T>(N / 2 > 0 ? N / 2 : 1);
         const CT* stw_cols = c.stage_tw<T>(N);
@@ -337,8 +368,12 @@ template <typename T> struct Pipe {
             band1 = N / 2 + pg->rmax;
             timed(c, s, ST_ROWS, [&] {
                 CK(L::rows_profile(prof, nr, Rmin, dR, dxy, std::cos(inc), pg->rmax, pg->central, N, tw, stw_rows, zt,
-                                   st, duv, s));
+                                   st, duv, s, ov ? C : -1));
             });
+        }
+        if (ov) {
+            CK(cudaStreamWaitEvent(s, ov->ev_uv, 0));
+            timed(c, s, ST_EXTENT, [&] { CK(L::extent(u, v, nd, N, duv, st, s)); });
         }
         // window layout: column k at win + k*N, rows [r0, r0+W) contiguous
         timed(c, s, ST_COLS, [&] {
@@ -392,7 +427,36 @@ template <typename T> struct Pipe {
         a.chi2_out = chi2_out;
         a.state = st;
         if (before_vis) before_vis();
-        if (nd > 0) timed(c, s, ST_VIS, [&] { CK(L::vis(a, s)); });
+        if (nd > 0 && ov) {
+            int total = 0;
+            for (int k = 0; k < nchunks; ++k)
+                total += L::vis_grid(std::max(1, chunk_begin(nd, nchunks, k + 1) - chunk_begin(nd, nchunks, k)));
+            CK(cudaEventRecord(c.ev_win, s));
+            CK(cudaStreamWaitEvent(c.vis2, c.ev_win, 0));
+            int off = 0;
+            for (int k = 0; k < nchunks; ++k) {
+                const int b0 = chunk_begin(nd, nchunks, k), b1 = chunk_begin(nd, nchunks, k + 1);
+                typename L::VisArgs ak = a;
+                ak.u = u + b0;
+                ak.v = v + b0;
+                ak.re = re ? re + b0 : nullptr;
+                ak.im = im ? im + b0 : nullptr;
+                ak.w = w ? w + b0 : nullptr;
+                ak.vis_out = vis_out ? vis_out + b0 : nullptr;
+                ak.nd = b1 - b0;
+                ak.base = b0;
+                ak.part_off = off;
+                ak.parts_total = total;
+                cudaStream_t sk = (k & 1) ? c.vis2 : s;
+                CK(cudaStreamWaitEvent(sk, ov->ev_chunk[k], 0));
+                CK(L::vis(ak, sk));
+                off += L::vis_grid(std::max(1, ak.nd));
+            }
+            CK(cudaEventRecord(c.ev_vis2, c.vis2));
+            CK(cudaStreamWaitEvent(s, c.ev_vis2, 0));
+        } else if (nd > 0) {
+            timed(c, s, ST_VIS, [&] { CK(L::vis(a, s)); });
+        }
     }
 };
 
@@ -521,15 +585,31 @@ template <typename T> struct Api {
         T* im_d = as<T>(c.im, (size_t)nd);
         T* w_d = as<T>(c.w, (size_t)nd);
         DevState* st = as<DevState>(c.state, 1);
-        const auto obs = upload_obs<T>(c, s, re_d, re, im_d, im, w_d, w, nd);
-        timed(c, s, ST_H2D, [&] {
-            h2d(I_d, I, sizeof(T) * (size_t)nr, s);
-            h2d(u_d, u, sizeof(T) * (size_t)nd, s);
-            h2d(v_d, v, sizeof(T) * (size_t)nd, s);
-        });
+        // the profile first (host-to-device copies run in the order they
+        // are issued, whatever their stream), then the uploads on the side
+        // stream: (u, v) first so that the extent pass can start early, then
+        // the observations chunk by chunk; meanwhile the row pass (which needs
+        // only the profile) runs on `s`
+        timed(c, s, ST_H2D, [&] { h2d(I_d, I, sizeof(T) * (size_t)nr, s); });
         CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
+        Overlap ov;
+        ov.ev_uv = c.ev_uv;
+        ov.nchunks = std::max(1, std::min(Ctx::kMaxChunks, nd >> 18));
+        ov.ev_chunk = c.ev_chunk;
+        CK(cudaEventRecord(c.ev_side_start, s));
+        CK(cudaStreamWaitEvent(c.side, c.ev_side_start, 0));
+        h2d(u_d, u, sizeof(T) * (size_t)nd, c.side);
+        h2d(v_d, v, sizeof(T) * (size_t)nd, c.side);
+        CK(cudaEventRecord(c.ev_uv, c.side));
+        for (int k = 0; k < ov.nchunks; ++k) {
+            const size_t b0 = (size_t)chunk_begin(nd, ov.nchunks, k), n = (size_t)chunk_begin(nd, ov.nchunks, k + 1) - b0;
+            h2d(re_d + b0, re + b0, sizeof(T) * n, c.side);
+            h2d(im_d + b0, im + b0, sizeof(T) * n, c.side);
+            h2d(w_d + b0, w + b0, sizeof(T) * n, c.side);
+            CK(cudaEventRecord(c.ev_chunk[k], c.side));
+        }
         Pipe<T>::enqueue(c, s, N, (double)duv, nullptr, I_d, nr, Rmin, dR, dxy, inc, &pg, 1.0, dRA, dDec, PA, nd, u_d,
-                         v_d, re_d, im_d, w_d, nullptr, true, nullptr, st, false, obs);
+                         v_d, re_d, im_d, w_d, nullptr, true, nullptr, st, false, std::function<void()>(), &ov);
         finish(c, st);
         *chi2 = (T)c.host_state->chi2;
     }

@@ -418,22 +418,28 @@ __device__ __forceinline__ double block_sum(double x, double* sh) {
 // to arrive sums the partials with all its threads: thread i takes partials
 // i, i + blockDim, ... in order, then a fixed-shape tree (block_sum).  The
 // summation order depends only on the grid size, so results are reproducible.
+// A reduction split over several launches (chunks of the visibilities, which
+// may run concurrently on two streams): the launch whose blocks are numbered
+// from `off` writes partials[off + b], every block of every launch takes a
+// ticket, and the block that takes ticket nparts - 1 (nparts = all launches'
+// blocks) sums partials[0, nparts) in the fixed order.
 __device__ __forceinline__ void grid_finish(double block_total, double* partials, DevState* st,
-                                            double* extra_out = nullptr) {
+                                            double* extra_out = nullptr, int off = 0, int nparts_all = 0) {
     __shared__ bool last;
     __shared__ double sh2[32];
+    const unsigned nparts = nparts_all > 0 ? (unsigned)nparts_all : gridDim.x;
     if (threadIdx.x == 0) {
-        partials[blockIdx.x] = block_total;
+        partials[off + blockIdx.x] = block_total;
         __threadfence();
         const unsigned t = atomicAdd(&st->ticket, 1u);
-        last = (t == gridDim.x - 1);
+        last = (t == nparts - 1);
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
     double s = 0.0;
     const volatile double* p = partials;
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) s += p[b];
+    for (unsigned b = threadIdx.x; b < nparts; b += blockDim.x) s += p[b];
     s = block_sum(s, sh2);
     if (threadIdx.x == 0) {
         st->chi2 = s;

@@ -96,10 +96,12 @@ template <typename T> struct Launch {
     // tw: exp(-2 pi i m / N), m in [0, N); stw: stage twiddles of the length-N/2 row FFT
     static cudaError_t rows_image(const T* image, int N, const CT* tw, const CT* stw, CT* zt, int host_K,
                                   const DevState* state, double duv, bool row_sign, cudaStream_t s);
-    // row pass fused with the profile sweep: only rows [N/2 - rmax, N/2 + rmax) are nonzero
+    // row pass fused with the profile sweep: only rows [N/2 - rmax, N/2 + rmax) are nonzero.
+    // Writes columns [0, kcols), or the device window's K columns when kcols < 0
+    // (kcols >= 0 lets the pass run before the extent pass).
     static cudaError_t rows_profile(const T* intensity, int nr, double Rmin, double dR, double dxy, double cos_inc,
                                     int rmax, double central_value, int N, const CT* tw, const CT* stw, CT* zt,
-                                    const DevState* state, double duv, cudaStream_t s);
+                                    const DevState* state, double duv, cudaStream_t s, int kcols = -1);
     // column pass: column FFTs of zt (rows outside [band0, band1) are zero) and
     // write rows [r0, r0+W) of columns [0, K) to out[(r - r0)*s_row + k*s_col],
     // times (-1)^(r + k + N/2) if out_sign.  host_K/host_r0/host_W >= 0 override
@@ -157,6 +159,13 @@ template <typename T> struct Launch {
         double* partials;    // chi2 partials (null: no chi2)
         double* chi2_out;    // optional extra copy of the final chi2 (device)
         DevState* state;
+        // one chunk of a set of launches over the visibilities: u..w and
+        // vis_out point at the chunk, `base` is its first visibility's index,
+        // `part_off` the first chi2 partial slot of this launch and
+        // `parts_total` the blocks of all the set's launches (0: this launch alone)
+        int base = 0;
+        int part_off = 0;
+        int parts_total = 0;
     };
     static cudaError_t vis(const VisArgs& a, cudaStream_t s);
     // Cell-major copy of the window for the visibility gather: one record of

@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(MAXT) rows_profile_kernel(const T* __restrict_
                                                             T inv_dR, T dxy, T inv_cos_inc, int rmax, T central, int N,
                                                             const C2<T>* __restrict__ tw,
                                                             const C2<T>* __restrict__ stw, C2<T>* __restrict__ zt,
-                                                            const DevState* __restrict__ st, double duv) {
+                                                            const DevState* __restrict__ st, double duv, int kcols) {
     using CT = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CT* buf = reinterpret_cast<CT*>(smem_raw);
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(MAXT) rows_profile_kernel(const T* __restrict_
     }
     __syncthreads();
     block_fft<T, E>(buf, M, ilog2(M), stw);
-    const int K = st->win_K;
+    const int K = kcols >= 0 ? kcols : st->win_K;
     const T sgn = (I & 1) ? (T)-1 : (T)1;
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
         CT x = real_split<T>(buf, M, k, tw);
@@ -601,7 +601,7 @@ __global__ void __launch_bounds__(256) vis_kernel(typename Launch<T>::VisArgs a)
         const CT o1 = has1 ? vis_point<T, REALQ>(a, w, u1, v1, &e1) : CT{(T)0, (T)0};
         if (e0 | e1) {
             err |= e0 | e1;
-            if (err_idx < 0) err_idx = e0 ? i0 : i1;
+            if (err_idx < 0) err_idx = (long long)a.base + (e0 ? i0 : i1);
         }
         if (VISOUT) {
             a.vis_out[i0] = o0;
@@ -620,7 +620,7 @@ __global__ void __launch_bounds__(256) vis_kernel(typename Launch<T>::VisArgs a)
     }
     if (CHI2) {
         const double tot = block_sum((double)acc, sh);
-        grid_finish(tot, a.partials, a.state, a.chi2_out);
+        grid_finish(tot, a.partials, a.state, a.chi2_out, a.part_off, a.parts_total);
     }
 }
 
@@ -842,8 +842,9 @@ cudaError_t Launch<T>::rows_image(const T* image, int N, const CT* tw, const CT*
 template <typename T>
 cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, double dR, double dxy, double cos_inc,
                                     int rmax, double central_value, int N, const CT* tw, const CT* stw, CT* zt,
-                                    const DevState* state, double duv, cudaStream_t s) {
+                                    const DevState* state, double duv, cudaStream_t s, int kcols) {
     const int nrows = 2 * rmax;
+    if (kcols > N / 2 + 1) kcols = N / 2 + 1;
     if (nrows <= 0) return cudaSuccess;
     const T inv_cos = (T)(1.0 / cos_inc);
     if (is_pow2(N) && N <= max_fft_n_impl<T>() * 2) {
@@ -855,7 +856,8 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
             e = set_smem(kern, c.smem);
             if (e == cudaSuccess) {
                 kern<<<rmax + 1, c.threads, c.smem, s>>>(intensity, nr, (T)Rmin, (T)dR, (T)(1.0 / dR), (T)dxy,
-                                                         inv_cos, rmax, (T)central_value, N, tw, stw, zt, state, duv);
+                                                         inv_cos, rmax, (T)central_value, N, tw, stw, zt, state, duv,
+                                                         kcols);
                 e = cudaGetLastError();
             }
         });
@@ -865,7 +867,7 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
     cudaError_t e = set_smem(rows_direct_kernel<T>, sm);
     if (e != cudaSuccess) return e;
     rows_direct_kernel<T><<<nrows, 256, sm, s>>>(nullptr, N, N / 2 - rmax, intensity, nr, (T)Rmin, (T)dR, (T)dxy,
-                                                 inv_cos, rmax, (T)central_value, 1, tw, zt, -1, state, duv, 1);
+                                                 inv_cos, rmax, (T)central_value, 1, tw, zt, kcols, state, duv, 1);
     return cudaGetLastError();
 }
 
