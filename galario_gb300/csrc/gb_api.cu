@@ -125,7 +125,7 @@ struct Ctx {
     cudaStream_t vis2 = nullptr;
     cudaEvent_t ev_win = nullptr, ev_vis2 = nullptr;
     DevBuf state, partials, img, prof, u, v, re, im, w, vis, zt, win, amp, quad, urot, vrot;
-    double2* phase_tab = nullptr;  // table of the FP64 phase shift (PHASE_T + 1 entries)
+    double2* phase_tab = nullptr;  // table of the FP64 phase shift (PHASE_T entries)
     std::map<std::pair<int, int>, void*> tw;   // (N, sizeof(T)) -> table
     std::map<std::pair<int, int>, void*> stw;  // (L, sizeof(T)) -> stage twiddles
     DevState* host_state = nullptr;           // pinned mirror of DevState
@@ -160,15 +160,15 @@ struct Ctx {
         CK(cudaEventCreateWithFlags(&ev_vis2, cudaEventDisableTiming));
         for (auto& e : ev_chunk) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         CK(cudaMallocHost(&host_state, sizeof(DevState)));
-        // exp(2 pi i (j - T/2) / T), j in [0, T], evaluated in long double
-        std::vector<double2> h(PHASE_T + 1);
+        // exp(2 pi i j / T), j in [0, T), evaluated in long double
+        std::vector<double2> h(PHASE_T);
         const long double two_pi = 6.283185307179586476925286766559005768L;
-        for (int j = 0; j <= PHASE_T; ++j) {
-            long double a = two_pi * (long double)(j - PHASE_T / 2) / (long double)PHASE_T;
+        for (int j = 0; j < PHASE_T; ++j) {
+            long double a = two_pi * (long double)j / (long double)PHASE_T;
             h[(size_t)j] = make_double2((double)cosl(a), (double)sinl(a));
         }
-        CK(cudaMalloc(&phase_tab, sizeof(double2) * (PHASE_T + 1)));
-        CK(cudaMemcpy(phase_tab, h.data(), sizeof(double2) * (PHASE_T + 1), cudaMemcpyHostToDevice));
+        CK(cudaMalloc(&phase_tab, sizeof(double2) * PHASE_T));
+        CK(cudaMemcpy(phase_tab, h.data(), sizeof(double2) * PHASE_T, cudaMemcpyHostToDevice));
     }
     void release_all() {
         DevBuf* bufs[] = {&state, &partials, &img, &prof, &u, &v, &re, &im, &w, &vis, &zt, &win, &amp, &quad,

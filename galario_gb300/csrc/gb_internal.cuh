@@ -77,8 +77,8 @@ constexpr int QUAD_REC = 16;
 // cells of the quad buffer (2^21: 128 MiB in FP32, 256 MiB in FP64)
 constexpr long long QUAD_CAP = 1LL << 21;
 
-// size of the table of the table-driven sin/cos of the phase shift
-constexpr int PHASE_T = 1024;
+// size of the table of the table-driven sin/cos of the phase shift (a power of two)
+constexpr int PHASE_T = 65536;
 
 inline bool is_pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
 
@@ -124,7 +124,7 @@ template <typename T> struct Launch {
         const T* quads;      // cell-major records (see Launch::quads), or null: gather from spec/amp
         bool real_quads = false;  // quads hold 4 real corners per cell (real spectrum of a swept profile)
         long long quad_cap;  // capacity of quads in cells; larger windows gather from spec/amp
-        const double2* phase_tab;  // exp(2 pi i (j - PHASE_T/2) / PHASE_T), j in [0, PHASE_T]; FP64 path
+        const double2* phase_tab;  // exp(2 pi i j / PHASE_T), j in [0, PHASE_T); FP64 path
         long long s_row, s_col;
         int nrow, ncol;      // logical N and C of the full spectrum (flat-index semantics)
         int host_K, host_r0, host_W;  // window (>= 0) or derive from state
@@ -134,6 +134,11 @@ template <typename T> struct Launch {
         bool phase;          // dra != 0 || ddec != 0
         // derived on the host by finalize(): no per-thread FP64 set-up in the kernels
         double inv_duv, half_nrow;
+        // FP64 path: grid coordinates (a, c) = (u', v') / duv from (u, v) with
+        // cu = cos(PA)/duv, su = sin(PA)/duv; the phase u' dra + v' ddec as
+        // a dra_g + c ddec_g; vo_sign flips the sign bit of c for v_origin < 0
+        double cu_d, su_d, dra_g, ddec_g;
+        long long vo_sign;
         float half_nrow_f, v_origin_f;
         DF inv_duv_df, cpa, spa, dra_df, ddec_df;  // double-float copies for the FP32 path
         void finalize() {
@@ -145,6 +150,11 @@ template <typename T> struct Launch {
             };
             inv_duv = 1.0 / duv;
             half_nrow = (double)(nrow / 2);
+            cu_d = cos_pa * inv_duv;
+            su_d = sin_pa * inv_duv;
+            dra_g = dra * duv;
+            ddec_g = ddec * duv;
+            vo_sign = v_origin < 0 ? (long long)0x8000000000000000ULL : 0LL;
             half_nrow_f = (float)(nrow / 2);
             v_origin_f = (float)v_origin;
             inv_duv_df = split(inv_duv);

@@ -380,13 +380,14 @@ __device__ __forceinline__ bool interp_cell_real(const typename Launch<T>::VisAr
             yr[c] = __ldg(&a.spec[(long long)qc * a.s_row + (long long)cc[c] * a.s_col]).x;
         }
     }
-    const T d1 = (yr[0] + yr[2]) - (yr[1] + yr[3]);
-    const T zr = t * (q * d1) + (t * (yr[1] - yr[0]) + q * (yr[3] - yr[0])) + yr[0];
+    // the reference's bilinear forms (interpolate_core :782-812),
+    // y0 + t (y1 - y0) + q ((y3 - y0) + t (y0 - y1 + y2 - y3)), in fused
+    // multiply-adds: the signed corners (only the sign of z is used) and the moduli
+    const T f1 = yr[1] - yr[0], f3 = yr[3] - yr[0];
+    const T zr = fma(q, fma(t, (yr[2] - yr[3]) - f1, f3), fma(t, f1, yr[0]));
     const T m0 = fabs(yr[0]), m1 = fabs(yr[1]), m2 = fabs(yr[2]), m3 = fabs(yr[3]);
-    T amp = m0;
-    amp += (m3 - m0) * q;
-    amp += (m1 - m0) * t;
-    amp += (m0 - m1 + m2 - m3) * t * q;
+    const T e1 = m1 - m0, e3 = m3 - m0;
+    const T amp = fma(q, fma(t, (m2 - m3) - e1, e3), fma(t, e1, m0));
     *out = zr < (T)0 ? -amp : amp;
     return true;
 }
@@ -490,38 +491,46 @@ __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a,
     using CT = C2<T>;
     CT out = CT{(T)0, (T)0};
     if constexpr (sizeof(T) == 8) {
-        // FP64: index and phase in double, as the reference's double build
-        double ur = u_in, vr = v_in;
+        // FP64.  Grid coordinates of the rotated point, ga = u'/duv and
+        // gc = v'/duv, with cos(PA)/duv and sin(PA)/duv from the host (the
+        // reference divides u' by duv: same value to rounding).
+        double ga = u_in * a.inv_duv, gc = v_in * a.inv_duv;
         if (a.rotate) {
-            ur = u_in * a.cos_pa - v_in * a.sin_pa;
-            vr = u_in * a.sin_pa + v_in * a.cos_pa;
+            ga = fma(u_in, a.cu_d, -(v_in * a.su_d));
+            gc = fma(u_in, a.su_d, v_in * a.cu_d);
         }
-        if (!(isfinite(ur) && isfinite(vr))) {
-            *e = ERR_UV_NONFINITE;
+        // the Hermitian half: indu = |u'|/duv and v' -> v_origin sign(u') v'
+        // (sign(u') = copysign(1, u'), as the reference), as sign-bit operations
+        constexpr long long kSign = (long long)0x8000000000000000ULL, kExp = 0x7ff0000000000000LL;
+        const long long ba = __double_as_longlong(ga), bc = __double_as_longlong(gc);
+        const long long sa = ba & kSign;
+        const long long bu = ba ^ sa, bv = bc ^ sa ^ a.vo_sign;
+        // |indu|, |v'/duv| < 4 N as integer compares of the bit patterns of
+        // non-negative doubles (NaN and inf compare above every finite value)
+        const long long lim = __double_as_longlong(4.0 * a.nrow);
+        if (!(bu < lim && (bv & ~kSign) < lim)) {
+            *e = ((ba & kExp) == kExp || (bc & kExp) == kExp) ? ERR_UV_NONFINITE : ERR_UV_OUTSIDE;
             return out;
         }
-        const double indu = fabs(ur) * a.inv_duv;
-        const double sign_u = copysign(1.0, ur);
-        const double indv = a.half_nrow + a.v_origin * sign_u * vr * a.inv_duv;
-        if (!(indu < 4.0 * a.nrow && indv > -4.0 * a.nrow && indv < 4.0 * a.nrow)) {
-            *e = ERR_UV_OUTSIDE;
-            return out;
-        }
+        const double indu = __longlong_as_double(bu);
+        const double indv = a.half_nrow + __longlong_as_double(bv);
         const double fu = floor(indu), fv = floor(indv);
         if constexpr (REALQ) {
             T amp;
             if (interp_cell_real<T>(a, w, (int)fu, (int)fv, (T)(indu - fu), (T)(indv - fv), &amp, e)) {
                 out = CT{amp, (T)0};
                 if (a.phase) {
+                    // u' dra + v' ddec = ga (dra duv) + gc (ddec duv) cycles
                     double sn, cs;
-                    sincos2pi_tab(ur * a.dra + vr * a.ddec, a.phase_tab, &sn, &cs);
+                    sincos2pi_tab(fma(ga, a.dra_g, gc * a.ddec_g), a.phase_tab, &sn, &cs);
                     out = CT{amp * (T)cs, amp * (T)sn};
                 }
             }
-        } else if (interp_cell<T>(a, w, (int)fu, (int)fv, (T)(indu - fu), (T)(indv - fv), (T)sign_u, &out, e) &&
+        } else if (interp_cell<T>(a, w, (int)fu, (int)fv, (T)(indu - fu), (T)(indv - fv), sa ? (T)-1 : (T)1, &out,
+                                  e) &&
                    a.phase) {
             double sn, cs;
-            sincos2pi_tab(ur * a.dra + vr * a.ddec, a.phase_tab, &sn, &cs);
+            sincos2pi_tab(fma(ga, a.dra_g, gc * a.ddec_g), a.phase_tab, &sn, &cs);
             out = cmul(out, CT{(T)cs, (T)sn});
         }
     } else {
