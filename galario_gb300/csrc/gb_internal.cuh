@@ -13,6 +13,8 @@
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include <cstring>
 #include <stdint.h>
 
 namespace gbg {
@@ -138,7 +140,7 @@ template <typename T> struct Launch {
         // cu = cos(PA)/duv, su = sin(PA)/duv; the phase u' dra + v' ddec as
         // a dra_g + c ddec_g; vo_sign flips the sign bit of c for v_origin < 0
         double cu_d, su_d, dra_g, ddec_g;
-        long long vo_sign;
+        long long vo_sign, lim_bits;  // lim_bits: bit pattern of 4 N (coarse range check)
         float half_nrow_f, v_origin_f;
         DF inv_duv_df, cpa, spa, dra_df, ddec_df;  // double-float copies for the FP32 path
         void finalize() {
@@ -155,6 +157,8 @@ template <typename T> struct Launch {
             dra_g = dra * duv;
             ddec_g = ddec * duv;
             vo_sign = v_origin < 0 ? (long long)0x8000000000000000ULL : 0LL;
+            const double lim = 4.0 * nrow;
+            std::memcpy(&lim_bits, &lim, sizeof(lim));
             half_nrow_f = (float)(nrow / 2);
             v_origin_f = (float)v_origin;
             inv_duv_df = split(inv_duv);

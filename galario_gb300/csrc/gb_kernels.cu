@@ -254,13 +254,28 @@ __global__ void cols_direct_kernel(const C2<T>* __restrict__ zt, int N, int band
 // ---------------------------------------------------------------------------
 // dataset extent
 // ---------------------------------------------------------------------------
+// An upper bound of |x| as a float from the high word of a double, without
+// FP64 arithmetic: the exponent and the top 20 mantissa bits plus one unit of
+// the 20th bit (relative slack at most 2^-19).  NaN and inf give 0 (the
+// visibility pass flags them), |x| < 2^-126 gives 2^-126, |x| >= 2^128 gives inf.
+__device__ __forceinline__ float abs_bound_f(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x) & 0x7fffffffu;
+    const int e = (int)(hi >> 20);
+    if (e == 2047) return 0.f;
+    if (e < 1023 - 126) return 1.17549435e-38f;
+    if (e > 1023 + 127) return __uint_as_float(0x7f800000u);
+    return __uint_as_float((((unsigned)(e - 1023 + 127) << 23) | ((hi & 0xfffffu) << 3)) + 8u);
+}
+
 template <typename T>
 __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, int nd, int N, double duv,
                               DevState* st) {
-    // max(u^2 + v^2) in the input precision (NaN entries are ignored here and
-    // flagged by the visibility pass); the window adds a relative margin
-    // larger than the float rounding of this maximum
-    T mt = (T)0;
+    // max(u^2 + v^2) (NaN entries are ignored here and flagged by the
+    // visibility pass), in FP32: for FP64 inputs as the sum of squares of
+    // upper bounds of |u| and |v| (an upper bound itself: its rounding is far
+    // below the bounds' slack); the window adds a relative margin larger than
+    // the slack
+    float mt = 0.f;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     int done = 0;
     if ((reinterpret_cast<uintptr_t>(u) & 15) == 0 && (reinterpret_cast<uintptr_t>(v) & 15) == 0) {
@@ -272,10 +287,12 @@ __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, 
         const V* vv = reinterpret_cast<const V*>(v);
         auto acc = [&](const V& a, const V& b) {
             if constexpr (sizeof(T) == 4) {
-                mt = fmax(mt, fmax(fmax(a.x * a.x + b.x * b.x, a.y * a.y + b.y * b.y),
-                                   fmax(a.z * a.z + b.z * b.z, a.w * a.w + b.w * b.w)));
+                mt = fmaxf(mt, fmaxf(fmaxf(a.x * a.x + b.x * b.x, a.y * a.y + b.y * b.y),
+                                     fmaxf(a.z * a.z + b.z * b.z, a.w * a.w + b.w * b.w)));
             } else {
-                mt = fmax(mt, fmax(a.x * a.x + b.x * b.x, a.y * a.y + b.y * b.y));
+                const float ax = abs_bound_f(a.x), ay = abs_bound_f(a.y);
+                const float bx = abs_bound_f(b.x), by = abs_bound_f(b.y);
+                mt = fmaxf(mt, fmaxf(fmaf(ax, ax, bx * bx), fmaf(ay, ay, by * by)));
             }
         };
         int i = tid;
@@ -289,10 +306,15 @@ __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, 
     }
     for (int i = done + tid; i < nd; i += nth) {
         const T a = __ldg(&u[i]), b = __ldg(&v[i]);
-        mt = fmax(mt, a * a + b * b);
+        if constexpr (sizeof(T) == 4) {
+            mt = fmaxf(mt, a * a + b * b);
+        } else {
+            const float ab = abs_bound_f(a), bb = abs_bound_f(b);
+            mt = fmaxf(mt, fmaf(ab, ab, bb * bb));
+        }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mt = fmax(mt, __shfl_xor_sync(0xffffffffu, mt, o));
+    for (int o = 16; o > 0; o >>= 1) mt = fmaxf(mt, __shfl_xor_sync(0xffffffffu, mt, o));
     double m = (double)mt;
     __shared__ double sh[32];  // one per warp, blocks of up to 1024 threads
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = m;
@@ -507,8 +529,7 @@ __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a,
         const long long bu = ba ^ sa, bv = bc ^ sa ^ a.vo_sign;
         // |indu|, |v'/duv| < 4 N as integer compares of the bit patterns of
         // non-negative doubles (NaN and inf compare above every finite value)
-        const long long lim = __double_as_longlong(4.0 * a.nrow);
-        if (!(bu < lim && (bv & ~kSign) < lim)) {
+        if (!(bu < a.lim_bits && (bv & ~kSign) < a.lim_bits)) {
             *e = ((ba & kExp) == kExp || (bc & kExp) == kExp) ? ERR_UV_NONFINITE : ERR_UV_OUTSIDE;
             return out;
         }
