@@ -2096,8 +2096,12 @@ static void batch_run(const BatchCall& call) {
                 for (int e : fft_candidates(g.N)) col_shapes.push_back(e + kTmaCols);
             sh.e_rows = tu.best(fft_candidates(g.M), [&](int e) { sh.e_rows = e; run_all(); });
             sh.e_cols = tu.best(col_shapes, [&](int e) { sh.e_cols = e; run_all(); });
-            sh.pts = tu.best(real ? std::vector<int>{2, 4, 8} : std::vector<int>{2, 4},
-                             [&](int p) { sh.pts = p; run_all(); });
+            // the visibility pass alone decides its shape (the spectrum passes
+            // before it do not depend on it and only add noise): one complete
+            // call sets up the window, then each candidate reruns the pass
+            // (the gradient records it accumulates are zeroed by the next call)
+            run_all();
+            sh.pts = tu.best(real ? std::vector<int>{2, 4, 8} : std::vector<int>{2, 4}, [&](int p) { vis(p); });
             if (grad) {
                 sh.e_colsT = tu.best(fft_candidates(g.N), [&](int e) { sh.e_colsT = e; run_all(); });
                 sh.e_rowsT = tu.best(fft_candidates(g.M), [&](int e) { sh.e_rowsT = e; run_all(); });

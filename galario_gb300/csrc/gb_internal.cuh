@@ -194,7 +194,8 @@ template <typename T> struct Launch {
     static cudaError_t quads(const CT* spec, const T* amp, long long s_row, long long s_col, int C,
                              const DevState* state, T* quads, long long cap, int host_K, int host_r0, int host_W,
                              cudaStream_t s);
-    // records of a real spectrum: the 4 real corners of every cell (4 T per cell)
+    // records of a real spectrum: the 4 real corners of every cell (4 T per cell;
+    // in FP64 followed by their 4 FP32 copies, 48 bytes per cell)
     static cudaError_t quads_real(const CT* spec, long long s_row, long long s_col, int C, const DevState* state,
                                   T* quads, long long cap, cudaStream_t s);
     static int vis_grid(int nd);

@@ -351,6 +351,18 @@ __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, 
 // amp * exp(i sign_u arg z) = (amp * sign(z), 0).  Corners come from the real
 // cell records, or from the window's real parts when it exceeds the record
 // capacity.  Writes the real result to *out.
+// Reals per record of a real spectrum: the 4 corners, and in FP64 also their
+// FP32 copies (4 floats in the space of 2 doubles; 48-byte records).
+template <typename T> __host__ __device__ constexpr int real_rec() { return sizeof(T) == 8 ? 6 : 4; }
+
+// t in [0, 1) (FP64) to FP32 without a conversion instruction: the high word
+// of t + 1 holds the exponent of 1 and the top 20 fraction bits of t, so the
+// float built from them is 1 + t truncated to 20 bits (error below 2^-20).
+__device__ __forceinline__ float frac_to_f(double t) {
+    const unsigned hi = (unsigned)__double2hiint(t + 1.0);
+    return __uint_as_float(0x3f800000u | ((hi & 0xfffffu) << 3)) - 1.0f;
+}
+
 template <typename T>
 __device__ __forceinline__ bool interp_cell_real(const typename Launch<T>::VisArgs& a, const Window& w, int fu,
                                                  int fv, T q, T t, T* out, unsigned* err) {
@@ -368,13 +380,15 @@ __device__ __forceinline__ bool interp_cell_real(const typename Launch<T>::VisAr
     }
     const int qq = r0 - w.r0;
     T yr[4];
+    float yf[4];
+    bool have_f = false;
     if ((long long)w.K * w.W <= a.quad_cap) {
         const bool inside = wrap ? (w.K == C && qq >= 0 && qq < w.W - 2) : (c0 < w.K - 1 && qq >= 0 && qq < w.W - 1);
         if (!inside) {
             *err |= ERR_WINDOW;
             return false;
         }
-        const T* rec = a.quads + ((long long)c0 * w.W + qq) * 4;
+        const T* rec = a.quads + ((long long)c0 * w.W + qq) * real_rec<T>();
         if constexpr (sizeof(T) == 4) {
             const float4 p0 = __ldg(reinterpret_cast<const float4*>(rec));
             yr[0] = p0.x;
@@ -384,10 +398,16 @@ __device__ __forceinline__ bool interp_cell_real(const typename Launch<T>::VisAr
         } else {
             const double2 p0 = __ldg(reinterpret_cast<const double2*>(rec));
             const double2 p1 = __ldg(reinterpret_cast<const double2*>(rec) + 1);
+            const float4 pf = __ldg(reinterpret_cast<const float4*>(rec + 4));
             yr[0] = p0.x;
             yr[1] = p0.y;
             yr[2] = p1.x;
             yr[3] = p1.y;
+            yf[0] = pf.x;
+            yf[1] = pf.y;
+            yf[2] = pf.z;
+            yf[3] = pf.w;
+            have_f = true;
         }
     } else {
         const int rr[4] = {r0, r0 + 1, r_last, wrap ? r0 + 1 : r0};
@@ -404,13 +424,35 @@ __device__ __forceinline__ bool interp_cell_real(const typename Launch<T>::VisAr
     }
     // the reference's bilinear forms (interpolate_core :782-812),
     // y0 + t (y1 - y0) + q ((y3 - y0) + t (y0 - y1 + y2 - y3)), in fused
-    // multiply-adds: the signed corners (only the sign of z is used) and the moduli
-    const T f1 = yr[1] - yr[0], f3 = yr[3] - yr[0];
-    const T zr = fma(q, fma(t, (yr[2] - yr[3]) - f1, f3), fma(t, f1, yr[0]));
+    // multiply-adds: the moduli, and the signed corners z of which only the
+    // sign is used
     const T m0 = fabs(yr[0]), m1 = fabs(yr[1]), m2 = fabs(yr[2]), m3 = fabs(yr[3]);
     const T e1 = m1 - m0, e3 = m3 - m0;
     const T amp = fma(q, fma(t, (m2 - m3) - e1, e3), fma(t, e1, m0));
-    *out = zr < (T)0 ? -amp : amp;
+    bool neg;
+    bool decided = false;
+    if constexpr (sizeof(T) == 8) {
+        if (have_f) {
+            // FP32 estimate of z from the records' FP32 corners and the
+            // fractions truncated to 20 bits: its error is below
+            // (8 * 2^-24 + 2 * 2^-20) * sum|y| < 2.5e-6 sum|y|, so a value
+            // beyond 4e-6 sum|y| has the sign of the FP64 z
+            const float tf = frac_to_f(t), qf = frac_to_f(q);
+            const float g1 = yf[1] - yf[0], g3 = yf[3] - yf[0];
+            const float zf = fmaf(qf, fmaf(tf, (yf[2] - yf[3]) - g1, g3), fmaf(tf, g1, yf[0]));
+            const float mag = (fabsf(yf[0]) + fabsf(yf[1])) + (fabsf(yf[2]) + fabsf(yf[3]));
+            if (fabsf(zf) > 4e-6f * mag) {
+                neg = zf < 0.f;
+                decided = true;
+            }
+        }
+    }
+    if (!decided) {
+        const T f1 = yr[1] - yr[0], f3 = yr[3] - yr[0];
+        const T zr = fma(q, fma(t, (yr[2] - yr[3]) - f1, f3), fma(t, f1, yr[0]));
+        neg = zr < (T)0;
+    }
+    *out = neg ? -amp : amp;
     return true;
 }
 
@@ -602,7 +644,7 @@ __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a,
 // Grid-stride over the visibilities, two independent points per iteration so
 // their load -> gather chains overlap.
 template <typename T, bool CHI2, bool VISOUT, bool REALQ>
-__global__ void __launch_bounds__(256) vis_kernel(typename Launch<T>::VisArgs a) {
+__global__ void __launch_bounds__(256, (sizeof(T) == 8 && REALQ) ? 4 : 1) vis_kernel(typename Launch<T>::VisArgs a) {
     using CT = C2<T>;
     __shared__ double sh[32];
     const Window w = get_window(a.host_K, a.host_r0, a.host_W, a.state);
@@ -702,9 +744,13 @@ __global__ void quad_real_kernel(const C2<T>* __restrict__ spec, long long s_row
 #pragma unroll
         for (int c = 0; c < 4; ++c) ok = ok && rr[c] < w.W && cc[c] < w.K;
         if (!ok) continue;
-        T* rec = quads + e * 4;
+        T* rec = quads + e * real_rec<T>();
 #pragma unroll
-        for (int c = 0; c < 4; ++c) rec[c] = spec[(long long)rr[c] * s_row + (long long)cc[c] * s_col].x;
+        for (int c = 0; c < 4; ++c) {
+            const T y = spec[(long long)rr[c] * s_row + (long long)cc[c] * s_col].x;
+            rec[c] = y;
+            if constexpr (sizeof(T) == 8) reinterpret_cast<float*>(rec + 4)[c] = (float)y;
+        }
     }
 }
 
