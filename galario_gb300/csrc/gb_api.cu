@@ -361,6 +361,9 @@ template <typename T> struct Pipe {
         int band0 = 0, band1 = N;
         const CT* stw_rows = c.stage_tw<T>(N / 2 > 0 ? N / 2 : 1);
         const CT* stw_cols = c.stage_tw<T>(N);
+        // FP64 swept profiles: rows and columns as even-sequence transforms (FFT
+        // length N/4); the FP32 passes are faster as paired transforms
+        const CT* stw_q = (!img && sizeof(T) == 8 && even_dft_ok<T>(N)) ? c.stage_tw<T>(N / 4) : nullptr;
         if (img) {
             timed(c, s, ST_ROWS, [&] { CK(L::rows_image(img, N, tw, stw_rows, zt, -1, st, duv, true, s)); });
         } else {
@@ -368,7 +371,7 @@ template <typename T> struct Pipe {
             band1 = N / 2 + pg->rmax;
             timed(c, s, ST_ROWS, [&] {
                 CK(L::rows_profile(prof, nr, Rmin, dR, dxy, std::cos(inc), pg->rmax, pg->central, N, tw, stw_rows, zt,
-                                   st, duv, s, ov ? C : -1));
+                                   st, duv, s, ov ? C : -1, stw_q));
             });
         }
         if (ov) {
@@ -380,7 +383,7 @@ template <typename T> struct Pipe {
             if (img)
                 CK(L::cols(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, -1, -1, -1, st, duv, true, s));
             else
-                CK(L::cols_profile(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, st, duv, s));
+                CK(L::cols_profile(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, st, duv, s, stw_q));
         });
         // a swept profile's spectrum is real: 4 real corners per cell record
         const bool real_spec = img == nullptr;

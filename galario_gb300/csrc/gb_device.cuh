@@ -414,6 +414,108 @@ __device__ __forceinline__ double block_sum(double x, double* sh) {
     return s;  // valid in thread 0
 }
 
+// ---------------------------------------------------------------------------
+// Transform of a real sequence even about index 0 (a DCT-I): with period
+// N = 2n, s[0] = x_0, s[+-j] = x_j (0 < j < n), s[n] = x_n,
+//   C_k = sum_J s[J] exp(-2 pi i J k / N)
+//       = x_0 + (-1)^k x_n + 2 sum_{j=1}^{n-1} x_j cos(pi j k / n),  k in [0, kmax],
+// from one complex FFT of length n/2 (a quarter of N).  With
+//   y_0 = (x_0 + x_n)/2,  y_j = (x_j + x_{n-j})/2 - sin(pi j/n) (x_j - x_{n-j}),
+// and Y = DFT_n(y): the part of y odd about n/2 drops out of Re Y_k and the
+// part even about n/2 out of Im Y_k, and the product-to-sum identity
+// 2 sin(a) sin(2ka) = cos((2k-1)a) - cos((2k+1)a) gives
+//   C_{2k} = 2 Re Y_k,   C_{2k+1} = C_{2k-1} - 2 Im Y_k,
+//   C_1 = (x_0 - x_n) + 2 sum_{j=1}^{n-1} x_j cos(pi j/n),
+// so the odd outputs are C_1 minus twice a prefix sum of Im Y (the cosine
+// transform algorithm of Numerical Recipes' cosft1, derived here with the
+// forward sign of this code).  Y comes from the length-n/2 complex FFT of
+// y_{2m} + i y_{2m+1} and the even/odd split.  Block-wide: blockDim.x =
+// n / (2E) threads, at least 32.
+//   xs   x_0 .. x_{nnz-1} in shared memory (x_j = 0 for nnz <= j < n); xn = x_n
+//   twN  exp(-2 pi i j / N), j < N;  stw: stage twiddles of the length-n/2 FFT
+//   buf  fft_slots(n/2) complex;  im: n/2 + 1 reals;  out: kmax + 1 reals
+//        (may alias xs: xs is read only before the transform)
+// Sums are in FP64 in a fixed order (reproducible).
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ C2<T> real_split_stride2(const C2<T>* Z, int M, int k, const C2<T>* __restrict__ twN) {
+    using CT = C2<T>;
+    const CT za = Z[sp(k == M ? 0 : k)];
+    const CT zb = Z[sp(k == 0 ? 0 : M - k)];
+    const T h = (T)0.5;
+    const CT e = CT{h * (za.x + zb.x), h * (za.y - zb.y)};
+    const T pr = za.x - zb.x, pi = za.y + zb.y;
+    const CT o = CT{h * pi, -h * pr};
+    const CT w = __ldg(&twN[2 * k]);  // exp(-2 pi i k / n), n = 2M
+    return cadd(e, cmul(o, w));
+}
+
+template <typename T, int E>
+__device__ void even_dft_block(const T* xs, int nnz, T xn, int n, const C2<T>* __restrict__ twN,
+                               const C2<T>* __restrict__ stw, C2<T>* buf, T* im, T* out, int kmax) {
+    using CT = C2<T>;
+    __shared__ double sh[32];
+    __shared__ double c1_sh;
+    const int t = threadIdx.x, bd = blockDim.x;
+    const int M = n / 2;
+    // C_1
+    double acc = 0.0;
+    for (int j = 1 + t; j < nnz; j += bd) acc += (double)xs[j] * (double)__ldg(&twN[j]).x;
+    const double s = block_sum(acc, sh);
+    if (t == 0) c1_sh = ((nnz > 0 ? (double)xs[0] : 0.0) - (double)xn) + 2.0 * s;
+    // y packed as z_m = y_{2m} + i y_{2m+1}
+    for (int m = t; m < M; m += bd) {
+        T y[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int j = 2 * m + h;
+            if (j == 0) {
+                y[h] = (T)0.5 * ((nnz > 0 ? xs[0] : (T)0) + xn);
+            } else {
+                const T xj = j < nnz ? xs[j] : (T)0;
+                const T xm = (n - j) < nnz ? xs[n - j] : (T)0;
+                const T sj = -__ldg(&twN[j]).y;  // sin(pi j / n)
+                y[h] = (T)0.5 * (xj + xm) - sj * (xj - xm);
+            }
+        }
+        buf[sp(m)] = CT{y[0], y[1]};
+    }
+    __syncthreads();
+    block_fft<T, E>(buf, M, 31 - __clz(M), stw);
+    __syncthreads();
+    const int kh = kmax / 2;  // Y_k for k <= kh gives C_0 .. C_kmax
+    for (int k = t; k <= kh; k += bd) {
+        const CT Y = real_split_stride2<T>(buf, M, k, twN);
+        out[2 * k] = (T)2 * Y.x;
+        im[k] = Y.y;
+    }
+    __syncthreads();
+    // odd outputs: C_{2k+1} = C_1 - 2 sum_{i=1}^{k} Im Y_i (warp 0: contiguous
+    // segments per lane, a shuffle scan of the segment sums, then the segments)
+    if (t < 32) {
+        const int L = (kmax - 1) / 2;  // odd outputs 3, 5, .., need prefixes up to L
+        const int seg = (L + 31) / 32;
+        const int b0 = 1 + t * seg, b1 = min(b0 + seg, L + 1);
+        double loc = 0.0;
+        for (int i = b0; i < b1; ++i) loc += (double)im[i];
+        double incl = loc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (t >= o) incl += v;
+        }
+        double run = __shfl_up_sync(0xffffffffu, incl, 1);
+        if (t == 0) run = 0.0;
+        const double c1 = c1_sh;
+        if (t == 0 && kmax >= 1) out[1] = (T)c1;
+        for (int i = b0; i < b1; ++i) {
+            run += (double)im[i];
+            out[2 * i + 1] = (T)(c1 - 2.0 * run);
+        }
+    }
+    __syncthreads();
+}
+
 // Deterministic grid reduction: each block writes its partial, the last block
 // to arrive sums the partials with all its threads: thread i takes partials
 // i, i + blockDim, ... in order, then a fixed-shape tree (block_sum).  The
@@ -595,6 +697,19 @@ template <typename T> FftCfg<T> fft_cfg(int M) {
 
 // values per thread of the shared-memory FFT of length M in precision T
 template <typename T> inline int fft_e(int M) { return fft_cfg<T>(M).E; }
+
+// shared memory of the even-sequence transform kernels of length N: the
+// length-N/4 FFT buffer, the N/2 + 1 half sequence and N/4 + 1 scratch reals
+template <typename T> inline size_t even_dft_smem(int N) {
+    return sizeof(C2<T>) * fft_slots(N / 4) + sizeof(T) * ((size_t)N / 2 + 1) + sizeof(T) * ((size_t)N / 4 + 1);
+}
+// the even-sequence transforms need a power-of-two N, a length-N/4 FFT with
+// at least one warp of threads, and shared memory within a block's limit
+template <typename T> inline bool even_dft_ok(int N) {
+    if (!is_pow2(N) || N < 16 || N / 4 > max_fft_n_impl<T>()) return false;
+    const FftCfg<T> c = fft_cfg<T>(N / 4);
+    return c.threads >= 32 && c.threads <= 1024 && even_dft_smem<T>(N) <= 200 * 1024;
+}
 
 template <typename K> cudaError_t set_smem(K kernel, size_t smem) {
     if (smem > 48 * 1024) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

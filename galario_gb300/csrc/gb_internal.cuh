@@ -103,7 +103,8 @@ template <typename T> struct Launch {
     // (kcols >= 0 lets the pass run before the extent pass).
     static cudaError_t rows_profile(const T* intensity, int nr, double Rmin, double dR, double dxy, double cos_inc,
                                     int rmax, double central_value, int N, const CT* tw, const CT* stw, CT* zt,
-                                    const DevState* state, double duv, cudaStream_t s, int kcols = -1);
+                                    const DevState* state, double duv, cudaStream_t s, int kcols = -1,
+                                    const CT* stw4 = nullptr);
     // column pass: column FFTs of zt (rows outside [band0, band1) are zero) and
     // write rows [r0, r0+W) of columns [0, K) to out[(r - r0)*s_row + k*s_col],
     // times (-1)^(r + k + N/2) if out_sign.  host_K/host_r0/host_W >= 0 override
@@ -112,9 +113,11 @@ template <typename T> struct Launch {
     // pass gathers amplitudes instead of recomputing 4 moduli per point.
     // column pass of a swept profile (real, even columns): two columns per
     // complex transform; device window; output sign applied
+    // stw4 (stage twiddles of length N/4; row pass too): the even-sequence
+    // transform of one column per block, for the N where even_dft_ok holds
     static cudaError_t cols_profile(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
                                     T* amp_out, long long s_row, long long s_col, const DevState* state, double duv,
-                                    cudaStream_t s);
+                                    cudaStream_t s, const CT* stw4 = nullptr);
     // stw: stage twiddles of the length-N column FFT
     static cudaError_t cols(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
                             T* amp_out, long long s_row, long long s_col, int host_K, int host_r0, int host_W,

@@ -175,6 +175,98 @@ __global__ void __launch_bounds__(MAXT) cols_pair_kernel(const C2<T>* __restrict
 }
 
 // ---------------------------------------------------------------------------
+// Swept profiles as even sequences (even_dft_block): the swept image is even
+// in x about column N/2 and in y about row N/2, so each image row and each
+// spectrum column is a DCT-I of its half (n + 1 = N/2 + 1 values), computed
+// with a complex FFT of length N/4 instead of N/2 (paired row transform) or
+// N (paired column transform).  Shared memory: the FFT buffer, the half
+// sequence (reused for the transform's output) and the Im Y scratch.
+// ---------------------------------------------------------------------------
+// Row pass: block a transforms image row I = N/2 - a (and its mirror N/2 + a):
+// X[k] = sum_J x[J] exp(-2 pi i J k / N) = (-1)^k C_k, C the even transform
+// of f(j) = sweep(|x| = j dxy), j in [0, n]; written times the row sign.
+template <typename T, int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) rows_profile_dct_kernel(const T* __restrict__ intensity, int nr, T Rmin, T dR,
+                                                                T inv_dR, T dxy, T inv_cos_inc, int rmax, T central,
+                                                                int N, const C2<T>* __restrict__ tw,
+                                                                const C2<T>* __restrict__ stw4, C2<T>* __restrict__ zt,
+                                                                const DevState* __restrict__ st, int kcols) {
+    using CT = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = N / 2, M = N / 4;
+    CT* buf = reinterpret_cast<CT*>(smem_raw);
+    T* xs = reinterpret_cast<T*>(buf + fft_slots(M));  // n + 1 values, then the output C_k
+    T* im = xs + (n + 1);
+    const int off = N / 2 - rmax;
+    const int a = blockIdx.x;
+    const int I = N / 2 - a;
+    const bool mirror = a > 0 && a < rmax;
+    const int I2 = N / 2 + a;
+    const T sr_to_px = dxy * dxy;
+    const int nnz = rmax < n ? rmax : n;
+    for (int j = threadIdx.x; j < nnz; j += blockDim.x) {
+        T v = sweep_pixel<T>(I, N / 2 - j, intensity, nr, Rmin, dR, inv_dR, dxy, inv_cos_inc, rmax, off, sr_to_px);
+        if (I == N / 2 && j == 0) v = central;  // reference central_pixel_d :1075-1079
+        xs[j] = v;
+    }
+    // x_n: column 0 (x = n dxy) lies in the box only when rmax reaches n
+    const T xn = rmax >= n ? sweep_pixel<T>(I, 0, intensity, nr, Rmin, dR, inv_dR, dxy, inv_cos_inc, rmax, off,
+                                            sr_to_px)
+                           : (T)0;
+    __syncthreads();
+    int K = kcols >= 0 ? kcols : st->win_K;
+    if (K > n + 1) K = n + 1;
+    if (K <= 0) return;  // uniform
+    even_dft_block<T, E>(xs, nnz, xn, n, tw, stw4, buf, im, xs, K - 1);
+    const T sgn = (I & 1) ? (T)-1 : (T)1;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        const T c = (k & 1) ? -xs[k] : xs[k];
+        const CT y = CT{sgn * c, (T)0};
+        zt[(size_t)k * N + I] = y;
+        if (mirror) zt[(size_t)k * N + I2] = y;
+    }
+}
+
+// Column pass: column k (with the row signs of the row pass) is even about
+// row N/2; undoing the signs gives the even sequence x'_j = zt[N/2 + j]
+// (-1)^(N/2+j), and the window value at row r is (-1)^k C'_|r - N/2| (the
+// output sign (-1)^(r+k+N/2) included).  One column per block.
+template <typename T, int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) cols_profile_dct_kernel(const C2<T>* __restrict__ zt, int N, int rmax,
+                                                                const C2<T>* __restrict__ tw,
+                                                                const C2<T>* __restrict__ stw4, C2<T>* __restrict__ out,
+                                                                T* __restrict__ amp_out, long long s_row,
+                                                                long long s_col, const DevState* __restrict__ st) {
+    using CT = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const Window w = get_window(-1, -1, -1, st);
+    const int k = blockIdx.x;
+    if (k >= w.K) return;  // uniform for the whole block
+    const int n = N / 2, M = N / 4;
+    CT* buf = reinterpret_cast<CT*>(smem_raw);
+    T* xs = reinterpret_cast<T*>(buf + fft_slots(M));
+    T* im = xs + (n + 1);
+    const CT* col = zt + (size_t)k * N;
+    const int nnz = rmax < n ? rmax : n;
+    for (int j = threadIdx.x; j < nnz; j += blockDim.x) {
+        const T v = __ldg(&col[N / 2 + j]).x;
+        xs[j] = ((N / 2 + j) & 1) ? -v : v;
+    }
+    const T xn = rmax >= n ? __ldg(&col[0]).x : (T)0;  // row 0 = N/2 - n, sign (+1)
+    __syncthreads();
+    const int dmax = max(N / 2 - w.r0, w.r0 + w.W - 1 - N / 2);
+    even_dft_block<T, E>(xs, nnz, xn, n, tw, stw4, buf, im, xs, dmax);
+    const T ks = (k & 1) ? (T)-1 : (T)1;
+    for (int q = threadIdx.x; q < w.W; q += blockDim.x) {
+        const int d = abs(w.r0 + q - N / 2);
+        const T f = ks * xs[d];
+        const long long o = (long long)q * s_row + (long long)k * s_col;
+        out[o] = CT{f, (T)0};
+        amp_out[o] = fabs(f);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // direct-DFT fallbacks for lengths the shared-memory FFT does not handle
 // (non powers of two, or too long for shared memory); tw has N entries.
 // ---------------------------------------------------------------------------
@@ -880,6 +972,13 @@ cudaError_t Launch<T>::extent(const T* u, const T* v, int nd, int N, double duv,
         else if ((THR) <= 512) { constexpr int TT = 512; __VA_ARGS__; }                    \
         else { constexpr int TT = 1024; __VA_ARGS__; }                                     \
     }
+// E = 8 or 16 only (the even-sequence transforms: at least 32 threads)
+#define GBG_DISPATCH_E816(E_, THR, ...)                                           \
+    switch (E_) {                                                                 \
+        case 8: GBG_CASE_T(8, THR, __VA_ARGS__) break;                            \
+        case 16: GBG_CASE_T(16, THR, __VA_ARGS__) break;                          \
+        default: return cudaErrorInvalidValue;                                    \
+    }
 #define GBG_DISPATCH_E(E_, THR, ...)                                              \
     switch (E_) {                                                                 \
         case 1: { constexpr int EE = 1; constexpr int TT = 256; __VA_ARGS__; } break; \
@@ -918,11 +1017,26 @@ cudaError_t Launch<T>::rows_image(const T* image, int N, const CT* tw, const CT*
 template <typename T>
 cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, double dR, double dxy, double cos_inc,
                                     int rmax, double central_value, int N, const CT* tw, const CT* stw, CT* zt,
-                                    const DevState* state, double duv, cudaStream_t s, int kcols) {
+                                    const DevState* state, double duv, cudaStream_t s, int kcols, const CT* stw4) {
     const int nrows = 2 * rmax;
     if (kcols > N / 2 + 1) kcols = N / 2 + 1;
     if (nrows <= 0) return cudaSuccess;
     const T inv_cos = (T)(1.0 / cos_inc);
+    if (stw4 && even_dft_ok<T>(N)) {
+        FftCfg<T> c = fft_cfg<T>(N / 4);
+        const size_t sm = even_dft_smem<T>(N);
+        cudaError_t e = cudaSuccess;
+        GBG_DISPATCH_E816(c.E, c.threads, {
+            auto kern = rows_profile_dct_kernel<T, EE, TT>;
+            e = set_smem(kern, sm);
+            if (e == cudaSuccess) {
+                kern<<<rmax + 1, c.threads, sm, s>>>(intensity, nr, (T)Rmin, (T)dR, (T)(1.0 / dR), (T)dxy, inv_cos,
+                                                     rmax, (T)central_value, N, tw, stw4, zt, state, kcols);
+                e = cudaGetLastError();
+            }
+        });
+        return e;
+    }
     if (is_pow2(N) && N <= max_fft_n_impl<T>() * 2) {
         const int M = N / 2;
         FftCfg<T> c = fft_cfg<T>(M);
@@ -950,7 +1064,22 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
 template <typename T>
 cudaError_t Launch<T>::cols_profile(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
                                     T* amp_out, long long s_row, long long s_col, const DevState* state, double duv,
-                                    cudaStream_t s) {
+                                    cudaStream_t s, const CT* stw4) {
+    if (stw4 && amp_out && even_dft_ok<T>(N)) {
+        FftCfg<T> c = fft_cfg<T>(N / 4);
+        const size_t sm = even_dft_smem<T>(N);
+        const int rmax = N / 2 - band0;  // the band is [N/2 - rmax, N/2 + rmax)
+        cudaError_t e = cudaSuccess;
+        GBG_DISPATCH_E816(c.E, c.threads, {
+            auto kern = cols_profile_dct_kernel<T, EE, TT>;
+            e = set_smem(kern, sm);
+            if (e == cudaSuccess) {
+                kern<<<N / 2 + 1, c.threads, sm, s>>>(zt, N, rmax, tw, stw4, out, amp_out, s_row, s_col, state);
+                e = cudaGetLastError();
+            }
+        });
+        return e;
+    }
     if (is_pow2(N) && N <= max_fft_n_impl<T>() && amp_out) {
         const int C = N / 2 + 1;
         FftCfg<T> c = fft_cfg<T>(N);

@@ -298,3 +298,69 @@ def test_concurrent_host_threads(g):
     with ThreadPoolExecutor(max_workers=4) as ex:
         par = list(ex.map(run, range(8)))
     assert par == seq  # the same launches in the same order per call: bit-identical
+
+
+def test_profile_sign_near_zero_crossings(g, orc):
+    """The FP64 profile path takes the sign of the interpolated real spectrum
+    value z from an FP32 estimate and recomputes it in FP64 when the estimate
+    is within its error bound of zero.  Points placed 1e-9, 1e-6 and 1e-3 of a
+    cell beside the zero crossings of z along the u axis (v = 0, where z is
+    linear in the cell fraction) exercise both branches; a wrong sign would
+    flip a visibility of full amplitude.  The real parts are compared: the
+    reference's value there also carries an imaginary part amp * Im z / Re z,
+    the rounding-level imaginary part of its FFT over a vanishing real part,
+    which the real-spectrum path does not have."""
+    nxy, dxy = 512, 0.02 * arcsec
+    Rmin, dR, nr = 1e-4 * arcsec, 1e-3 * arcsec, 4000
+    R = Rmin + dR * np.arange(nr)
+    I = 1e10 * np.exp(-0.5 * ((R - 1.0 * arcsec) / (0.1 * arcsec)) ** 2)
+    duv = 1 / (nxy * dxy)
+    kmax = int(0.45 * nxy / 2)
+    # at v = 0 and a whole cell index the interpolation returns the corner itself
+    uk = np.arange(1, kmax + 1) * duv
+    yk = orc["double"].sampleProfile(I, Rmin, dR, nxy, dxy, uk, np.zeros_like(uk)).real
+    u = []
+    scale = np.abs(yk).max()
+    for k in range(len(yk) - 1):
+        a, b = yk[k], yk[k + 1]
+        if a * b < 0 and min(abs(a), abs(b)) > 1e-6 * scale:
+            qs = a / (a - b)  # z = a + q (b - a) vanishes at q = a / (a - b)
+            for d in (1e-9, -1e-9, 1e-6, -1e-6, 1e-3, -1e-3):
+                q = qs + d
+                if 0 < q < 1:
+                    u.append((k + 1 + q) * duv)
+    assert len(u) >= 24, len(u)
+    u = np.array(u)
+    v = np.zeros_like(u)
+    vg = g.double.sampleProfile(I, Rmin, dR, nxy, dxy, u, v)
+    vo = orc["double"].sampleProfile(I, Rmin, dR, nxy, dxy, u, v)
+    assert np.array_equal(np.sign(vg.real), np.sign(vo.real))
+    assert rel_max(vg.real, vo.real) <= DP_V
+    assert np.all(vg.imag == 0)
+
+
+def test_chunked_host_pointer_chi2_profile(g, orc):
+    """A host-pointer chi2Profile of more than 2^19 visibilities uploads and
+    evaluates them in chunks on two streams (one chi2 reduction over all
+    chunks): same chi2 as the oracle, and an invalid point of a later chunk is
+    reported with its index in the whole array."""
+    nxy, dxy = 512, 0.02 * arcsec
+    Rmin, dR, nr = 1e-4 * arcsec, 1e-3 * arcsec, 4000
+    R = Rmin + dR * np.arange(nr)
+    I = 1e10 * np.exp(-0.5 * ((R - 0.8 * arcsec) / (0.15 * arcsec)) ** 2)
+    duv = 1 / (nxy * dxy)
+    nd = 3 * (1 << 18) + 123  # three chunks of uneven length
+    u, v = uv_log_uniform(nd, 0.5 * duv, 0.45 * nxy / 2 * duv, seed=11)
+    re, im, w = _obs(nd, seed=12)
+    kw = dict(inc=30 * deg, PA=0.7, dRA=0.02 * arcsec, dDec=0.01 * arcsec)
+    cg = g.double.chi2Profile(I, Rmin, dR, nxy, dxy, u, v, re, im, w, **kw)
+    co = orc["double"].chi2Profile(I, Rmin, dR, nxy, dxy, u, v, re, im, w, **kw)
+    assert abs(cg - co) / abs(co) <= DP_CHI2
+    # deterministic: the same call again gives the same bits
+    assert g.double.chi2Profile(I, Rmin, dR, nxy, dxy, u, v, re, im, w, **kw) == cg
+    bad = u.copy()
+    bad[700001] = np.nan
+    with pytest.raises(ValueError, match="not finite.*index 700001"):
+        g.double.chi2Profile(I, Rmin, dR, nxy, dxy, bad, v, re, im, w, **kw)
+    # the context stays usable afterwards
+    assert g.double.chi2Profile(I, Rmin, dR, nxy, dxy, u, v, re, im, w, **kw) == cg
