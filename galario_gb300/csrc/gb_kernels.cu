@@ -447,12 +447,43 @@ __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, 
 // FP32 copies (4 floats in the space of 2 doubles; 48-byte records).
 template <typename T> __host__ __device__ constexpr int real_rec() { return sizeof(T) == 8 ? 6 : 4; }
 
-// t in [0, 1) (FP64) to FP32 without a conversion instruction: the high word
-// of t + 1 holds the exponent of 1 and the top 20 fraction bits of t, so the
-// float built from them is 1 + t truncated to 20 bits (error below 2^-20).
+// t in [0, 1) (FP64) to FP32 by integer operations on its bit pattern
+// (exponent rebiased, mantissa truncated to 23 bits: relative error below
+// 2^-23); values below 2^-126 give 0.
 __device__ __forceinline__ float frac_to_f(double t) {
-    const unsigned hi = (unsigned)__double2hiint(t + 1.0);
-    return __uint_as_float(0x3f800000u | ((hi & 0xfffffu) << 3)) - 1.0f;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+    const int e = (int)(b >> 52) - 1023;
+    if (e < -126) return 0.f;
+    return __uint_as_float(((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+}
+
+// floor and fraction of x in [0, 2^30) by integer operations on the bit
+// pattern, exactly (the FP64 pipe, the bound of this kernel, is not used):
+// the integer part is the significand shifted right by 52 - e, the fraction
+// the remaining bits, renormalised with a leading-zero count.  Returns false
+// (and leaves the FP64 path to the caller) outside that range.
+__device__ __forceinline__ bool floor_frac_bits(double x, int* fl, double* frac) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    if (b >> 63) return false;  // negative (or -0)
+    const int e = (int)(b >> 52) - 1023;
+    if (e > 29) return false;
+    if (e < 0) {  // x < 1 (and x = 0)
+        *fl = 0;
+        *frac = x;
+        return true;
+    }
+    const unsigned long long m = (b & 0xfffffffffffffULL) | 0x10000000000000ULL;
+    const int sh = 52 - e;
+    *fl = (int)(m >> sh);
+    const unsigned long long f = m & ((1ULL << sh) - 1ULL);  // fraction = f 2^-sh
+    if (f == 0ULL) {
+        *frac = 0.0;
+        return true;
+    }
+    const int p = 63 - __clzll((long long)f);  // top bit of f: fraction in [2^(p-sh), 2^(p-sh+1))
+    const unsigned long long mant = (f << (52 - p)) & 0xfffffffffffffULL;
+    *frac = __longlong_as_double((long long)((((unsigned long long)(p - sh + 1023)) << 52) | mant));
+    return true;
 }
 
 template <typename T>
@@ -526,8 +557,8 @@ __device__ __forceinline__ bool interp_cell_real(const typename Launch<T>::VisAr
     if constexpr (sizeof(T) == 8) {
         if (have_f) {
             // FP32 estimate of z from the records' FP32 corners and the
-            // fractions truncated to 20 bits: its error is below
-            // (8 * 2^-24 + 2 * 2^-20) * sum|y| < 2.5e-6 sum|y|, so a value
+            // fractions truncated to FP32: its error is below
+            // (8 * 2^-24 + 2 * 2^-23) * sum|y| < 7.2e-7 sum|y|, so a value
             // beyond 4e-6 sum|y| has the sign of the FP64 z
             const float tf = frac_to_f(t), qf = frac_to_f(q);
             const float g1 = yf[1] - yf[0], g3 = yf[3] - yf[0];
@@ -669,10 +700,23 @@ __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a,
         }
         const double indu = __longlong_as_double(bu);
         const double indv = a.half_nrow + __longlong_as_double(bv);
-        const double fu = floor(indu), fv = floor(indv);
+        // cell and fractions: integer operations on the bit patterns (exact),
+        // FP64 floor only for a negative indv (a point outside the spectrum)
+        int ifu, ifv;
+        double qf, tf;
+        if (!floor_frac_bits(indu, &ifu, &qf)) {
+            const double f = floor(indu);
+            ifu = (int)f;
+            qf = indu - f;
+        }
+        if (!floor_frac_bits(indv, &ifv, &tf)) {
+            const double f = floor(indv);
+            ifv = (int)f;
+            tf = indv - f;
+        }
         if constexpr (REALQ) {
             T amp;
-            if (interp_cell_real<T>(a, w, (int)fu, (int)fv, (T)(indu - fu), (T)(indv - fv), &amp, e)) {
+            if (interp_cell_real<T>(a, w, ifu, ifv, (T)qf, (T)tf, &amp, e)) {
                 out = CT{amp, (T)0};
                 if (a.phase) {
                     // u' dra + v' ddec = ga (dra duv) + gc (ddec duv) cycles
@@ -681,8 +725,7 @@ __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a,
                     out = CT{amp * (T)cs, amp * (T)sn};
                 }
             }
-        } else if (interp_cell<T>(a, w, (int)fu, (int)fv, (T)(indu - fu), (T)(indv - fv), sa ? (T)-1 : (T)1, &out,
-                                  e) &&
+        } else if (interp_cell<T>(a, w, ifu, ifv, (T)qf, (T)tf, sa ? (T)-1 : (T)1, &out, e) &&
                    a.phase) {
             double sn, cs;
             sincos2pi_tab(fma(ga, a.dra_g, gc * a.ddec_g), a.phase_tab, &sn, &cs);
