@@ -127,7 +127,7 @@ struct Ctx {
     DevBuf state, partials, img, prof, u, v, re, im, w, vis, zt, win, amp, quad, urot, vrot;
     double2* phase_tab = nullptr;  // table of the FP64 phase shift (PHASE_T entries)
     std::map<std::pair<int, int>, void*> tw;   // (N, sizeof(T)) -> table
-    std::map<std::pair<int, int>, void*> stw;  // (L, sizeof(T)) -> stage twiddles
+    std::map<std::pair<int, int>, void*> stw;  // (L * 32 + E, sizeof(T)) -> stage twiddles
     DevState* host_state = nullptr;           // pinned mirror of DevState
     // optional per-stage CUDA-event timing (galario_stage_timing)
     bool timing = false;
@@ -180,11 +180,13 @@ struct Ctx {
         stw.clear();
     }
     // stage twiddles of the shared-memory FFT of length L (power of two), cached per (L, precision)
-    template <typename T> const C2<T>* stage_tw(int L) {
-        auto key = std::make_pair(L, (int)sizeof(T));
+    // stage twiddles of the length-L FFT with E values per thread (E <= 0: fft_e)
+    template <typename T> const C2<T>* stage_tw(int L, int E = 0) {
+        if (E <= 0) E = fft_e<T>(L);
+        auto key = std::make_pair(L * 32 + E, (int)sizeof(T));
         auto it = stw.find(key);
         if (it != stw.end()) return static_cast<const C2<T>*>(it->second);
-        std::vector<C2<T>> h = stage_twiddles<T>(L, fft_e<T>(L));
+        std::vector<C2<T>> h = stage_twiddles<T>(L, E);
         void* d = nullptr;
         CK(cudaMalloc(&d, sizeof(C2<T>) * h.size()));
         CK(cudaMemcpy(d, h.data(), sizeof(C2<T>) * h.size(), cudaMemcpyHostToDevice));
@@ -363,7 +365,8 @@ template <typename T> struct Pipe {
         const CT* stw_cols = c.stage_tw<T>(N);
         // FP64 swept profiles: rows and columns as even-sequence transforms (FFT
         // length N/4); the FP32 passes are faster as paired transforms
-        const CT* stw_q = (!img && sizeof(T) == 8 && even_dft_ok<T>(N)) ? c.stage_tw<T>(N / 4) : nullptr;
+        const CT* stw_q =
+            (!img && sizeof(T) == 8 && even_dft_ok<T>(N)) ? c.stage_tw<T>(N / 4, even_dft_e<T>(N)) : nullptr;
         if (img) {
             timed(c, s, ST_ROWS, [&] { CK(L::rows_image(img, N, tw, stw_rows, zt, -1, st, duv, true, s)); });
         } else {

@@ -703,12 +703,15 @@ template <typename T> inline int fft_e(int M) { return fft_cfg<T>(M).E; }
 template <typename T> inline size_t even_dft_smem(int N) {
     return sizeof(C2<T>) * fft_slots(N / 4) + sizeof(T) * ((size_t)N / 2 + 1) + sizeof(T) * ((size_t)N / 4 + 1);
 }
+// values per thread of the even-sequence transforms' length-N/4 FFT (those
+// of the plain FFT; 4 per thread, with twice the warps, measured slower)
+template <typename T> inline int even_dft_e(int N) { return fft_cfg<T>(N / 4).E; }
 // the even-sequence transforms need a power-of-two N, a length-N/4 FFT with
 // at least one warp of threads, and shared memory within a block's limit
 template <typename T> inline bool even_dft_ok(int N) {
     if (!is_pow2(N) || N < 16 || N / 4 > max_fft_n_impl<T>()) return false;
-    const FftCfg<T> c = fft_cfg<T>(N / 4);
-    return c.threads >= 32 && c.threads <= 1024 && even_dft_smem<T>(N) <= 200 * 1024;
+    const int threads = (N / 4) / even_dft_e<T>(N);
+    return threads >= 32 && threads <= 1024 && even_dft_smem<T>(N) <= 200 * 1024;
 }
 
 template <typename K> cudaError_t set_smem(K kernel, size_t smem) {

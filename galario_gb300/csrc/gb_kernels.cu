@@ -672,9 +672,11 @@ __device__ __forceinline__ bool interp_cell(const typename Launch<T>::VisArgs& a
 }
 
 // One visibility: rotation, index, interpolation and phase shift.
+// parts (FP64 real spectrum): receives (A, cos, sin) with V = A (cos, sin),
+// so that the residual can be formed with fused multiply-adds
 template <typename T, bool REALQ>
 __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a, const Window& w, T u_in, T v_in,
-                                           unsigned* e) {
+                                           unsigned* e, T* parts = nullptr) {
     using CT = C2<T>;
     CT out = CT{(T)0, (T)0};
     if constexpr (sizeof(T) == 8) {
@@ -718,11 +720,16 @@ __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a,
             T amp;
             if (interp_cell_real<T>(a, w, ifu, ifv, (T)qf, (T)tf, &amp, e)) {
                 out = CT{amp, (T)0};
+                double sn = 0.0, cs = 1.0;
                 if (a.phase) {
                     // u' dra + v' ddec = ga (dra duv) + gc (ddec duv) cycles
-                    double sn, cs;
                     sincos2pi_tab(fma(ga, a.dra_g, gc * a.ddec_g), a.phase_tab, &sn, &cs);
                     out = CT{amp * (T)cs, amp * (T)sn};
+                }
+                if (parts) {
+                    parts[0] = amp;
+                    parts[1] = (T)cs;
+                    parts[2] = (T)sn;
                 }
             }
         } else if (interp_cell<T>(a, w, ifu, ifv, (T)qf, (T)tf, sa ? (T)-1 : (T)1, &out, e) &&
@@ -804,8 +811,11 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 8 && REALQ) ? 4 : 1) vis_ke
             }
         }
         unsigned e0 = 0u, e1 = 0u;
-        const CT o0 = vis_point<T, REALQ>(a, w, u0, v0, &e0);
-        const CT o1 = has1 ? vis_point<T, REALQ>(a, w, u1, v1, &e1) : CT{(T)0, (T)0};
+        // FP64 real spectrum: V = A (cos, sin) kept in parts, the residual in fused multiply-adds
+        constexpr bool kParts = CHI2 && REALQ && sizeof(T) == 8;
+        T p0[3] = {(T)0, (T)1, (T)0}, p1[3] = {(T)0, (T)1, (T)0};
+        const CT o0 = vis_point<T, REALQ>(a, w, u0, v0, &e0, kParts ? p0 : nullptr);
+        const CT o1 = has1 ? vis_point<T, REALQ>(a, w, u1, v1, &e1, kParts ? p1 : nullptr) : CT{(T)0, (T)0};
         if (e0 | e1) {
             err |= e0 | e1;
             if (err_idx < 0) err_idx = (long long)a.base + (e0 ? i0 : i1);
@@ -815,8 +825,18 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 8 && REALQ) ? 4 : 1) vis_ke
             if (has1) a.vis_out[i1] = o1;
         }
         if (CHI2) {
-            const T dr0 = o0.x - re0, di0 = o0.y - im0;
-            const T dr1 = o1.x - re1, di1 = o1.y - im1;
+            T dr0, di0, dr1, di1;
+            if constexpr (kParts) {
+                dr0 = fma(p0[0], p0[1], -re0);
+                di0 = fma(p0[0], p0[2], -im0);
+                dr1 = fma(p1[0], p1[1], -re1);
+                di1 = fma(p1[0], p1[2], -im1);
+            } else {
+                dr0 = o0.x - re0;
+                di0 = o0.y - im0;
+                dr1 = o1.x - re1;
+                di1 = o1.y - im1;
+            }
             acc += w0 * (dr0 * dr0 + di0 * di0);
             acc += w1 * (dr1 * dr1 + di1 * di1);  // w1 == 0 when i1 is past the end
         }
@@ -1066,7 +1086,9 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
     if (nrows <= 0) return cudaSuccess;
     const T inv_cos = (T)(1.0 / cos_inc);
     if (stw4 && even_dft_ok<T>(N)) {
-        FftCfg<T> c = fft_cfg<T>(N / 4);
+        FftCfg<T> c;
+        c.E = even_dft_e<T>(N);
+        c.threads = (N / 4) / c.E;
         const size_t sm = even_dft_smem<T>(N);
         cudaError_t e = cudaSuccess;
         GBG_DISPATCH_E816(c.E, c.threads, {
@@ -1109,7 +1131,9 @@ cudaError_t Launch<T>::cols_profile(const CT* zt, int N, int band0, int band1, c
                                     T* amp_out, long long s_row, long long s_col, const DevState* state, double duv,
                                     cudaStream_t s, const CT* stw4) {
     if (stw4 && amp_out && even_dft_ok<T>(N)) {
-        FftCfg<T> c = fft_cfg<T>(N / 4);
+        FftCfg<T> c;
+        c.E = even_dft_e<T>(N);
+        c.threads = (N / 4) / c.E;
         const size_t sm = even_dft_smem<T>(N);
         const int rmax = N / 2 - band0;  // the band is [N/2 - rmax, N/2 + rmax)
         cudaError_t e = cudaSuccess;
