@@ -333,6 +333,8 @@ struct Overlap {
     const cudaEvent_t* ev_chunk = nullptr;
 };
 // chunk c of nd visibilities in n chunks: [chunk_begin(nd, n, c), chunk_begin(nd, n, c + 1))
+// (equal sizes: chunks falling in size, so that less is left after the last
+// upload, measured no faster)
 inline int chunk_begin(int nd, int n, int c) { return (int)((long long)nd * c / n); }
 
 template <typename T> struct Pipe {

@@ -371,7 +371,7 @@ __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, 
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     int done = 0;
     if ((reinterpret_cast<uintptr_t>(u) & 15) == 0 && (reinterpret_cast<uintptr_t>(v) & 15) == 0) {
-        // 16-byte vector loads, two vectors of each array in flight per thread
+        // 16-byte vector loads
         using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
         constexpr int L = 16 / sizeof(T);
         const int nvec = nd / L;
@@ -388,12 +388,17 @@ __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, 
             }
         };
         int i = tid;
-        for (; i + nth < nvec; i += 2 * nth) {
-            const V a0 = __ldg(&uv[i]), b0 = __ldg(&vv[i]), a1 = __ldg(&uv[i + nth]), b1 = __ldg(&vv[i + nth]);
-            acc(a0, b0);
-            acc(a1, b1);
+        for (; i + 3 * nth < nvec; i += 4 * nth) {  // four vectors of each array in flight
+            V a[4], b[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                a[r] = __ldg(&uv[i + r * nth]);
+                b[r] = __ldg(&vv[i + r * nth]);
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r) acc(a[r], b[r]);
         }
-        if (i < nvec) acc(__ldg(&uv[i]), __ldg(&vv[i]));
+        for (; i < nvec; i += nth) acc(__ldg(&uv[i]), __ldg(&vv[i]));
         done = nvec * L;
     }
     for (int i = done + tid; i < nd; i += nth) {
