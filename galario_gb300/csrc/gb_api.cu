@@ -388,11 +388,12 @@ template <typename T> struct Pipe {
             if (img)
                 CK(L::cols(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, -1, -1, -1, st, duv, true, s));
             else
-                CK(L::cols_profile(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, st, duv, s, stw_q));
+                CK(L::cols_profile(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, st, duv, s, stw_q, quads, qcap));
         });
         // a swept profile's spectrum is real: 4 real corners per cell record
         const bool real_spec = img == nullptr;
         timed(c, s, ST_QUAD, [&] {
+            if (real_spec && stw_q) return;  // the even-sequence column pass wrote the records
             if (real_spec)
                 CK(L::quads_real(win, 1, N, C, st, quads, qcap, s));
             else

@@ -114,10 +114,13 @@ template <typename T> struct Launch {
     // column pass of a swept profile (real, even columns): two columns per
     // complex transform; device window; output sign applied
     // stw4 (stage twiddles of length N/4; row pass too): the even-sequence
-    // transform of one column per block, for the N where even_dft_ok holds
+    // transform of one column per block, for the N where even_dft_ok holds,
+    // which also writes the real cell records of quads_real into quads (when
+    // the window has at most quad_cap cells); returns whether it did
     static cudaError_t cols_profile(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
                                     T* amp_out, long long s_row, long long s_col, const DevState* state, double duv,
-                                    cudaStream_t s, const CT* stw4 = nullptr);
+                                    cudaStream_t s, const CT* stw4 = nullptr, T* quads = nullptr,
+                                    long long quad_cap = 0);
     // stw: stage twiddles of the length-N column FFT
     static cudaError_t cols(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
                             T* amp_out, long long s_row, long long s_col, int host_K, int host_r0, int host_W,

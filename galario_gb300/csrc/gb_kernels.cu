@@ -32,6 +32,10 @@ namespace gbg {
 
 namespace {
 
+// Reals per record of a real spectrum: the 4 corners, and in FP64 also their
+// FP32 copies (4 floats in the space of 2 doubles; 48-byte records).
+template <typename T> __host__ __device__ constexpr int real_rec() { return sizeof(T) == 8 ? 6 : 4; }
+
 // ---------------------------------------------------------------------------
 // row pass kernels
 // ---------------------------------------------------------------------------
@@ -236,7 +240,8 @@ __global__ void __launch_bounds__(MAXT) cols_profile_dct_kernel(const C2<T>* __r
                                                                 const C2<T>* __restrict__ tw,
                                                                 const C2<T>* __restrict__ stw4, C2<T>* __restrict__ out,
                                                                 T* __restrict__ amp_out, long long s_row,
-                                                                long long s_col, const DevState* __restrict__ st) {
+                                                                long long s_col, const DevState* __restrict__ st,
+                                                                T* __restrict__ quads, long long cap) {
     using CT = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Window w = get_window(-1, -1, -1, st);
@@ -257,12 +262,42 @@ __global__ void __launch_bounds__(MAXT) cols_profile_dct_kernel(const C2<T>* __r
     const int dmax = max(N / 2 - w.r0, w.r0 + w.W - 1 - N / 2);
     even_dft_block<T, E>(xs, nnz, xn, n, tw, stw4, buf, im, xs, dmax);
     const T ks = (k & 1) ? (T)-1 : (T)1;
+    // the cell records of quad_real_kernel, written here: this column's
+    // element (q, k) is corner y0 of cell (k, q), y1 of (k, q-1), y3 of
+    // (k-1, q) and y2 of (k-1, q-1); with the flat-index wrap of the last
+    // column (K = C), column 0 also gives y3 of cell (C-1, q-1) and y2 of
+    // (C-1, q-2).  A cell (kc, qc) exists for kc + 1 < K, qc + 1 < W, and the
+    // wrapped one (kc = C-1) for qc + 2 < W.
+    const int C = N / 2 + 1;
+    const bool recs = quads && (long long)w.K * w.W <= cap;
+    auto put = [&](int kc, int qc, int corner, T f) {
+        T* rec = quads + ((long long)kc * w.W + qc) * real_rec<T>();
+        rec[corner] = f;
+        if constexpr (sizeof(T) == 8) reinterpret_cast<float*>(rec + 4)[corner] = (float)f;
+    };
     for (int q = threadIdx.x; q < w.W; q += blockDim.x) {
         const int d = abs(w.r0 + q - N / 2);
         const T f = ks * xs[d];
         const long long o = (long long)q * s_row + (long long)k * s_col;
         out[o] = CT{f, (T)0};
         amp_out[o] = fabs(f);
+        if (recs) {
+            if (k + 1 < w.K && k + 1 < C) {  // cells (k, q) and (k, q-1), not wrapped
+                if (q + 1 < w.W) put(k, q, 0, f);
+                if (q >= 1) put(k, q - 1, 1, f);
+            } else if (k + 1 == C && k < w.K) {  // wrapped cells of the last column
+                if (q + 2 < w.W) put(k, q, 0, f);
+                if (q >= 1 && q + 1 < w.W) put(k, q - 1, 1, f);
+            }
+            if (k >= 1 && k < w.K) {  // cells (k-1, q) and (k-1, q-1)
+                if (q + 1 < w.W) put(k - 1, q, 3, f);
+                if (q >= 1) put(k - 1, q - 1, 2, f);
+            }
+            if (k == 0 && w.K == C) {  // column 0 completes the wrapped cells of column C-1
+                if (q >= 1 && q + 1 < w.W) put(C - 1, q - 1, 3, f);
+                if (q >= 2) put(C - 1, q - 2, 2, f);
+            }
+        }
     }
 }
 
@@ -448,10 +483,6 @@ __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, 
 // amp * exp(i sign_u arg z) = (amp * sign(z), 0).  Corners come from the real
 // cell records, or from the window's real parts when it exceeds the record
 // capacity.  Writes the real result to *out.
-// Reals per record of a real spectrum: the 4 corners, and in FP64 also their
-// FP32 copies (4 floats in the space of 2 doubles; 48-byte records).
-template <typename T> __host__ __device__ constexpr int real_rec() { return sizeof(T) == 8 ? 6 : 4; }
-
 // t in [0, 1) (FP64) to FP32 by integer operations on its bit pattern
 // (exponent rebiased, mantissa truncated to 23 bits: relative error below
 // 2^-23); values below 2^-126 give 0.
@@ -1134,7 +1165,7 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
 template <typename T>
 cudaError_t Launch<T>::cols_profile(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
                                     T* amp_out, long long s_row, long long s_col, const DevState* state, double duv,
-                                    cudaStream_t s, const CT* stw4) {
+                                    cudaStream_t s, const CT* stw4, T* quads, long long quad_cap) {
     if (stw4 && amp_out && even_dft_ok<T>(N)) {
         FftCfg<T> c;
         c.E = even_dft_e<T>(N);
@@ -1146,7 +1177,8 @@ cudaError_t Launch<T>::cols_profile(const CT* zt, int N, int band0, int band1, c
             auto kern = cols_profile_dct_kernel<T, EE, TT>;
             e = set_smem(kern, sm);
             if (e == cudaSuccess) {
-                kern<<<N / 2 + 1, c.threads, sm, s>>>(zt, N, rmax, tw, stw4, out, amp_out, s_row, s_col, state);
+                kern<<<N / 2 + 1, c.threads, sm, s>>>(zt, N, rmax, tw, stw4, out, amp_out, s_row, s_col, state,
+                                                       quads, quad_cap);
                 e = cudaGetLastError();
             }
         });

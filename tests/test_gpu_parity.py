@@ -364,3 +364,29 @@ def test_chunked_host_pointer_chi2_profile(g, orc):
         g.double.chi2Profile(I, Rmin, dR, nxy, dxy, bad, v, re, im, w, **kw)
     # the context stays usable afterwards
     assert g.double.chi2Profile(I, Rmin, dR, nxy, dxy, u, v, re, im, w, **kw) == cg
+
+
+def test_profile_records_full_window_and_wrap(g, orc):
+    """FP64 profiles at nxy >= 1024 take the even-sequence column pass, which
+    also writes the real cell records; with points beyond |u| = N/2 duv the
+    window spans every column (K = N/2 + 1) and the records of the last column
+    take their u + 1 corners from column 0 of the next rows, as the
+    reference's flat indexing does (src/galario.cpp:774-780)."""
+    nxy, dxy = 1024, 0.01 * arcsec
+    Rmin, dR, nr = 1e-4 * arcsec, 5e-4 * arcsec, 6000  # (dxy/2 - Rmin)/dR = 9.8 > 5
+    R = Rmin + dR * np.arange(nr)
+    I = 1e10 * np.exp(-0.5 * ((R - 0.5 * arcsec) / (0.2 * arcsec)) ** 2)
+    duv = 1 / (nxy * dxy)
+    rng = np.random.default_rng(13)
+    u = np.concatenate([rng.uniform(-0.49, 0.49, 3000) * nxy * duv,
+                        np.array([512.3, -512.6, 512.9, 600.2, 0.25, 511.5]) * duv])
+    v = np.concatenate([rng.uniform(-0.49, 0.49, 3000) * nxy * duv,
+                        np.array([3.2, -7.7, 0.4, 11.1, 0.3, -200.2]) * duv])
+    for kw in (dict(), dict(inc=0.5, dRA=0.01 * arcsec, dDec=-0.02 * arcsec)):
+        vg = g.double.sampleProfile(I, Rmin, dR, nxy, dxy, u, v, **kw)
+        vo = orc["double"].sampleProfile(I, Rmin, dR, nxy, dxy, u, v, **kw)
+        assert rel_max(vg.real, vo.real) <= DP_V
+        re, im, w = _obs(len(u), seed=14)
+        cg = g.double.chi2Profile(I, Rmin, dR, nxy, dxy, u, v, re, im, w, **kw)
+        co = orc["double"].chi2Profile(I, Rmin, dR, nxy, dxy, u, v, re, im, w, **kw)
+        assert abs(cg - co) / abs(co) <= DP_CHI2
