@@ -546,7 +546,7 @@ def run_ours(args):
                          "traffic_source": "profiles/dram_traffic.txt (ncu dram__bytes_read+write of one launch)",
                          "note": "FP64 arithmetic on GB300 runs at ~1.2 TFLOP/s; the FP64 kernels are "
                                  "FP64-issue-bound, not HBM-bound",
-                         "fp64_pipe_active": 0.848,
+                         "fp64_pipe_active": 0.852,
                          "fp64_pipe_source": "profiles/vis_kernel_f64_chi2Profile_nxy4096_nvis2M.md "
                                              "(ncu sm__pipe_fp64_cycles_active of the vis kernel)"},
             "stages_ms": {k: round(v, 4) for k, v in stages64.items()},
