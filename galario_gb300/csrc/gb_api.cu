@@ -160,12 +160,48 @@ struct Ctx {
         CK(cudaEventCreateWithFlags(&ev_vis2, cudaEventDisableTiming));
         for (auto& e : ev_chunk) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         CK(cudaMallocHost(&host_state, sizeof(DevState)));
-        // exp(2 pi i j / T), j in [0, T), evaluated in long double
+        // exp(2 pi i j / T), j in [0, T), as exp(2 pi i jh / 2^10) exp(2 pi i jl / T)
+        // with j = 2^10 jh + jl: the two factors of 2^10 entries each from long
+        // double, kept as double-double pairs, multiplied in double-double
+        // arithmetic (products by fma, Dekker/Knuth) and rounded once
         std::vector<double2> h(PHASE_T);
-        const long double two_pi = 6.283185307179586476925286766559005768L;
-        for (int j = 0; j < PHASE_T; ++j) {
-            long double a = two_pi * (long double)j / (long double)PHASE_T;
-            h[(size_t)j] = make_double2((double)cosl(a), (double)sinl(a));
+        {
+            constexpr int kLo = 1 << 10, kHi = PHASE_T / kLo;
+            const long double two_pi = 6.283185307179586476925286766559005768L;
+            struct DD {
+                double hi, lo;
+            };
+            auto dd = [](long double x) {
+                const double hi = (double)x;
+                return DD{hi, (double)(x - (long double)hi)};
+            };
+            std::vector<DD> ch(kHi), sh(kHi), cl(kLo), sl(kLo);
+            for (int i = 0; i < kHi; ++i) {
+                const long double a = two_pi * (long double)i / (long double)kHi;
+                ch[i] = dd(cosl(a));
+                sh[i] = dd(sinl(a));
+            }
+            for (int i = 0; i < kLo; ++i) {
+                const long double a = two_pi * (long double)i / (long double)PHASE_T;
+                cl[i] = dd(cosl(a));
+                sl[i] = dd(sinl(a));
+            }
+            auto mul = [](DD x, DD y) {  // x y to about 2^-104
+                const double p = x.hi * y.hi;
+                return DD{p, std::fma(x.hi, y.hi, -p) + (x.hi * y.lo + x.lo * y.hi)};
+            };
+            auto add = [](DD x, DD y) {  // two-sum of the high parts, then the low parts
+                const double s = x.hi + y.hi, bb = s - x.hi;
+                const double e = (x.hi - (s - bb)) + (y.hi - bb);
+                return DD{s, e + (x.lo + y.lo)};
+            };
+            auto neg = [](DD x) { return DD{-x.hi, -x.lo}; };
+            for (int jh = 0; jh < kHi; ++jh)
+                for (int jl = 0; jl < kLo; ++jl) {
+                    const DD c = add(mul(ch[jh], cl[jl]), neg(mul(sh[jh], sl[jl])));
+                    const DD sn = add(mul(sh[jh], cl[jl]), mul(ch[jh], sl[jl]));
+                    h[(size_t)jh * kLo + jl] = make_double2(c.hi + c.lo, sn.hi + sn.lo);
+                }
         }
         CK(cudaMalloc(&phase_tab, sizeof(double2) * PHASE_T));
         CK(cudaMemcpy(phase_tab, h.data(), sizeof(double2) * PHASE_T, cudaMemcpyHostToDevice));

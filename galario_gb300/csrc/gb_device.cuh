@@ -643,24 +643,24 @@ __device__ __forceinline__ void sincos2pi_df(DF ph, float* s, float* c) {
 
 
 // sin/cos(2 pi a), a in cycles, FP64, table-driven (Tang's method): a = m/T
-// + d with m = rint(a T) and |d| <= 1/(2T).  a T + 1.5 * 2^52 (exact product,
-// one rounding for |a T| < 2^51) holds m in its low mantissa bits, so the
-// table index m mod T comes from the bit pattern without a conversion;
-// d = a - m/T is exact (Sterbenz), x = 2 pi d with |x| <= pi/T = 4.8e-5, so
-// cos x = 1 - x^2/2 and sin x = x - x^3/6 are exact to < 2.2e-19 (the next
-// terms).  The table E[j] = exp(2 pi i j / T) is built on the host in long double.
+// + d with m = rint(a T) and |d| <= 1/(2T), T = 2^20.  a T + 1.5 * 2^52
+// (exact product, one rounding for |a T| < 2^51) holds m in its low mantissa
+// bits, so the table index m mod T comes from the bit pattern without a
+// conversion; d = a - m/T is exact (Sterbenz), x = 2 pi d with |x| <= pi/T =
+// 3.0e-6, so cos x = 1 - x^2/2 and sin x = x leave out at most x^3/6 < 4.5e-18
+// in absolute terms.  exp(2 pi i a) = E (1 - h + i x) with h = x^2/2:
+// cos = E.x - E.x h - E.y x, sin = E.y + E.x x - E.y h in fused multiply-adds.
+// The table E[j] = exp(2 pi i j / T) is built on the host (1 ulp).
 __device__ __forceinline__ void sincos2pi_tab(double a, const double2* __restrict__ tab, double* s, double* c) {
     constexpr double kMagic52 = 6755399441055744.0;  // 1.5 * 2^52
     const double r = fma(a, (double)PHASE_T, kMagic52);
     const int j = __double2loint(r) & (PHASE_T - 1);
     const double d = fma(r - kMagic52, -1.0 / (double)PHASE_T, a);
     const double x = d * 6.283185307179586476925286766559;
-    const double x2 = x * x;
-    const double cx = fma(x2, -0.5, 1.0);
-    const double sx = fma(x * x2, -1.0 / 6.0, x);
+    const double h = (0.5 * x) * x;
     const double2 e = __ldg(&tab[j]);
-    *c = fma(e.x, cx, -(e.y * sx));
-    *s = fma(e.x, sx, e.y * cx);
+    *c = fma(-e.x, h, fma(-e.y, x, e.x));
+    *s = fma(-e.y, h, fma(e.x, x, e.y));
 }
 // FP32 phase: argument in FP64 with exact range reduction, evaluated in FP32
 template <typename T> __device__ __forceinline__ void sincos2pi(double a, T* s, T* c);

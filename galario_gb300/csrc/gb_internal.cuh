@@ -80,7 +80,7 @@ constexpr int QUAD_REC = 16;
 constexpr long long QUAD_CAP = 1LL << 21;
 
 // size of the table of the table-driven sin/cos of the phase shift (a power of two)
-constexpr int PHASE_T = 65536;
+constexpr int PHASE_T = 1 << 20;
 
 inline bool is_pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
 
