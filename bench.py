@@ -39,6 +39,7 @@ from __future__ import annotations
 
 import argparse
 import csv
+import datetime
 import io
 import json
 import os
@@ -138,25 +139,33 @@ def algorithmic_bytes(wl: Workload, s: int):
 # clocks during the timed region
 # ---------------------------------------------------------------------------
 class ClockSampler:
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi sampling every 20 ms from start() to stop(); summary() keeps
+    the samples whose timestamps fall inside the marked timed regions."""
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.out = ""
+        self.windows = []
 
-    def __enter__(self):
+    def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.5)  # let the first samples come in before a timed region starts
         except (FileNotFoundError, OSError):
             self.proc = None
         return self
 
-    def __exit__(self, *exc):
-        self.out = ""
+    def mark(self, t0, t1):
+        """A timed region, as two datetime.now() values."""
+        self.windows.append((t0, t1))
+
+    def stop(self):
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -164,27 +173,33 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
                 self.out, _ = self.proc.communicate()
+            self.proc = None
 
     def summary(self):
-        if not getattr(self, "out", ""):
+        if not self.out:
             return None
+        import datetime
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for row in csv.reader(io.StringIO(self.out)):
-            if len(row) < 9:
+            if len(row) < 10:
                 continue
             try:
-                sm.append(float(row[1]))
-                mx.append(float(row[2]))
+                ts = datetime.datetime.strptime(row[0].strip(), "%Y/%m/%d %H:%M:%S.%f")
+                clk, cmax = float(row[2]), float(row[3])
             except ValueError:
                 continue
-            for n, val in zip(names, row[5:9]):
+            if not any(a <= ts <= b for a, b in self.windows):
+                continue
+            sm.append(clk)
+            mx.append(cmax)
+            for n, val in zip(names, row[6:10]):
                 if val.strip().lower() == "active":
                     reasons.add(n)
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
-                "reasons": sorted(reasons)}
+                "reasons": sorted(reasons), "regions": "the timed loops of the FP64, FP32 and end-to-end rates"}
 
 
 def profiled_traffic(stage: str, precision: str):
@@ -282,6 +297,9 @@ def run_ours(args):
     wl = Workload(seed=0)
     L = _lib.lib()
     dev = torch.device("cuda", local)
+    clock_sampler = ClockSampler(local)
+    if args.part == "all":
+        clock_sampler.start()
     # a dedicated stream: the library's kernels, the L2 flush and the timing
     # events are all ordered on it
     stream = torch.cuda.Stream(dev)
@@ -326,7 +344,8 @@ def run_ours(args):
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
-        with ClockSampler(local) as clk, torch.cuda.stream(stream):
+        with torch.cuda.stream(stream):
+            d0 = datetime.datetime.now()
             t0 = time.perf_counter()
             for a, b in evs:
                 flush.zero_()
@@ -335,6 +354,7 @@ def run_ours(args):
                 b.record(stream)
             torch.cuda.synchronize()
             wall = time.perf_counter() - t0
+            clock_sampler.mark(d0, datetime.datetime.now())
         if dist is not None:
             dist.barrier()
         ms = sum(a.elapsed_time(b) for a, b in evs)
@@ -348,7 +368,7 @@ def run_ours(args):
             raise RuntimeError("device error bits %d" % err.value)
         stages = {L.galario_stage_name(i).decode(): (ms_sum[i] / cnt[i] if cnt[i] else 0.0) for i in range(8)
                   if cnt[i]}
-        return ms, stages, float(chi2_d.item()), clk.summary(), wall
+        return ms, stages, float(chi2_d.item()), None, wall
 
     if args.part == "batched":  # profiling runs of the batched path: the FP64 chi2 from one public call
         chi2_64 = g.double.chi2Profile(wl.intensity, wl.Rmin, wl.dR, wl.nxy, wl.dxy, wl.u, wl.v, re, im, wl.w,
@@ -512,11 +532,15 @@ def run_ours(args):
     e2e_steps = args.steps
     if dist is not None:
         dist.barrier()
+    d0 = datetime.datetime.now()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         e2e_chi2 = g.double.chi2Profile(host["I"], wl.Rmin, wl.dR, wl.nxy, wl.dxy, host["u"], host["v"],
                                         host["re"], host["im"], host["w"], **wl.kw())
     e2e_t = time.perf_counter() - t0
+    clock_sampler.mark(d0, datetime.datetime.now())
+    clock_sampler.stop()
+    clocks = clock_sampler.summary()
     if dist is not None:
         t = torch.tensor([e2e_t], dtype=torch.float64, device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
