@@ -620,14 +620,6 @@ __device__ __forceinline__ void sincos2pi_quadrant(float d, unsigned j, float* s
     *c = __int_as_float(__float_as_int(co) ^ (int)(((j + 1u) & 2u) << 30));
 }
 
-// sin/cos(2 pi f) in FP32 for |f| <= 1/2 + tiny, without conversion
-// instructions: j = rint(4 f), d = f - j/4 (exact by Sterbenz).
-__device__ __forceinline__ void sincos2pi_f32(float f, float* s, float* c) {
-    const float r = __fmaf_rn(f, 4.f, kMagic);
-    const float d = __fmaf_rn(__fsub_rn(r, kMagic), -0.25f, f);
-    sincos2pi_quadrant(d, (unsigned)(__float_as_int(r) - kMagicBits), s, c);
-}
-
 // sin/cos(2 pi (hi + lo)) for a double-float argument in turns (|hi| < 2^41,
 // |lo| at most a few ulps of hi), all in FP32: exact reductions by a whole
 // multiple of 2^20 turns (|h| <= 2^19 afterwards) and by quarter turns, each
