@@ -419,7 +419,7 @@ def run_ours(args):
         return {"value": B * steps / (ms * 1e-3), "unit": UNIT, "B": B, "steps": steps, "dtype": "f32",
                 "gradient": "chi2 and dchi2/d(4096 profile samples, inc, PA, dRA, dDec) per model",
                 "ms_per_step": ms / steps, "rel_chi2_vs_f64": abs(chi2_b0 - chi2_64) / abs(chi2_64),
-                "gpu_launches_per_step": 11}
+                "gpu_launches_per_step": 10}
 
     # the multi-dataset workload: B single-ring profiles, nxy=2048, dxy=5e-3",
     # Rmin=1e-4", dR=4e-4", nr=4096; 8 visibility sets with nd_k ~ U[2e5, 3e6],
@@ -587,7 +587,8 @@ def run_ours(args):
                                        "of FFTW), first call dropped"},
             "parity": {"chi2_f64": chi2_64, "chi2_e2e": e2e_chi2, "chi2_cpu": chi2_cpu,
                        "rel_f64_vs_cpu": abs(chi2_64 - chi2_cpu) / abs(chi2_cpu)},
-            "gpu_launches": 5 * args.steps,
+            # per FP64 step: extent, rows, cols (+ cell records), vis (ncu launch list)
+            "gpu_launches": 4 * args.steps,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
