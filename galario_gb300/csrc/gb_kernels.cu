@@ -1121,6 +1121,7 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
     if (kcols > N / 2 + 1) kcols = N / 2 + 1;
     if (nrows <= 0) return cudaSuccess;
     const T inv_cos = (T)(1.0 / cos_inc);
+    if constexpr (sizeof(T) == 8) {  // the FP32 passes keep the paired transforms
     if (stw4 && even_dft_ok<T>(N)) {
         FftCfg<T> c;
         c.E = even_dft_e<T>(N);
@@ -1137,6 +1138,7 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
             }
         });
         return e;
+    }
     }
     if (is_pow2(N) && N <= max_fft_n_impl<T>() * 2) {
         const int M = N / 2;
@@ -1166,6 +1168,7 @@ template <typename T>
 cudaError_t Launch<T>::cols_profile(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
                                     T* amp_out, long long s_row, long long s_col, const DevState* state, double duv,
                                     cudaStream_t s, const CT* stw4, T* quads, long long quad_cap) {
+    if constexpr (sizeof(T) == 8) {  // the FP32 passes keep the paired transforms
     if (stw4 && amp_out && even_dft_ok<T>(N)) {
         FftCfg<T> c;
         c.E = even_dft_e<T>(N);
@@ -1183,6 +1186,7 @@ cudaError_t Launch<T>::cols_profile(const CT* zt, int N, int band0, int band1, c
             }
         });
         return e;
+    }
     }
     if (is_pow2(N) && N <= max_fft_n_impl<T>() && amp_out) {
         const int C = N / 2 + 1;
