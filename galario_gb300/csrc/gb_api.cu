@@ -28,6 +28,8 @@
 #include "gb_internal.cuh"
 
 namespace gbg {
+void noalloc_forget_scratch();  // gb_noalloc.cu
+
 namespace {
 
 thread_local std::string g_msg;
@@ -910,6 +912,7 @@ API int galario_init(void) {
 }
 API int galario_cleanup(void) {
     return guarded([&] {
+        gbg::noalloc_forget_scratch();
         std::lock_guard<std::mutex> lk(gbg::g_ctx_mu);
         for (auto& kv : gbg::g_ctx) {
             std::lock_guard<std::mutex> l2(kv.second->mu);

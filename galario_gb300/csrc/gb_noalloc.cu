@@ -24,9 +24,17 @@
 //
 // Set-up: the first call on each device, with that device current, looks up
 // the device address of the array (cudaGetSymbolAddress) and caches it; make
-// that first call before any stream capture on the device.
+// that first call before any stream capture on the device.  galario_cleanup()
+// forgets the cached addresses (call it after a cudaDeviceReset, which reloads
+// the library's device image, possibly elsewhere).
+//
+// vis_dev holds nd interleaved (re, im) doubles and is read 16 bytes at a
+// time, so it must be 16-byte aligned (a complex128 array is; a view that
+// starts at an odd double is not): a misaligned pointer is rejected with
+// GALARIO_EINVAL before anything is enqueued.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <mutex>
 #include <string>
 
@@ -133,6 +141,14 @@ int fail(int status, const std::string& msg) {
 
 }  // namespace
 
+namespace gbg {
+// galario_cleanup (gb_api.cu): forget the per-device scratch addresses
+void noalloc_forget_scratch() {
+    std::lock_guard<std::mutex> lk(g_setup_mu);
+    for (auto& p : g_scratch_ptr) p = nullptr;
+}
+}  // namespace gbg
+
 extern "C" __attribute__((visibility("default"))) int galario_reduce_chi2_noalloc_d(
     int nd, const double* re_dev, const double* im_dev, const double* vis_dev, const double* w_dev, double* chi2_dev,
     void* stream) {
@@ -150,6 +166,9 @@ extern "C" __attribute__((visibility("default"))) int galario_reduce_chi2_noallo
     }
     if (!re_dev || !im_dev || !vis_dev || !w_dev)
         return fail(GALARIO_EINVAL, "Error in reduce_chi2_noalloc: a device pointer is NULL");
+    if ((reinterpret_cast<std::uintptr_t>(vis_dev) & 15u) != 0)
+        return fail(GALARIO_EINVAL, "Error in reduce_chi2_noalloc: vis_dev must be 16-byte aligned "
+                                    "(nd interleaved (re, im) doubles)");
     NoAllocScratch* scratch = nullptr;
     cudaError_t e = scratch_for_current_device(&scratch);
     if (e != cudaSuccess)

@@ -133,13 +133,24 @@ int galario_device_status(unsigned int *err_bits);
  * default stream).  It calls no cudaMalloc/cudaFree: its scratch is a fixed
  * 32 KiB array inside the library's device image, held by every GPU that
  * loads the library until exit.
- *  - nd <= 16,777,216, otherwise GALARIO_EINVAL;
+ *  - re_dev, im_dev, w_dev: nd doubles; vis_dev: nd interleaved (re, im)
+ *    doubles, 16-byte aligned (as a complex128 array), otherwise
+ *    GALARIO_EINVAL;
+ *  - nd <= 16,777,216, otherwise GALARIO_EINVAL; nd == 0 writes 0;
  *  - the first call on a device (with it current) looks up the scratch
  *    address once; make that first call before any stream capture;
+ *    galario_cleanup() forgets the addresses (needed after cudaDeviceReset);
  *  - all calls share the scratch: calls whose kernels overlap on the GPU
  *    race; order them on one stream. */
 int galario_reduce_chi2_noalloc_d(int nd, const double *re_dev, const double *im_dev, const double *vis_dev,
                                   const double *w_dev, double *chi2_dev, void *stream);
+
+/* ---- measurement helper (no reference counterpart) ----
+ * FP64 fused multiply-add throughput of the current device in GFLOP/s (two
+ * flops per FMA; independent chains, 8 blocks of 256 threads per SM, best of
+ * five timed launches): the FP64-pipe peak that the double-precision kernels'
+ * roofline is quoted against.  Allocates and frees a small buffer. */
+int galario_measure_fp64_peak(double *gflops);
 
 /* ---- stage timing (no reference counterpart; the reference's compile-time
  * GALARIO_TIMING prints, src/galario.cpp:64-87,275-315, become queryable

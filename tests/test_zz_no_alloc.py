@@ -58,6 +58,52 @@ def test_no_alloc_reduce_matches_regular_entry_point_twice():
         assert abs(got - expected) / abs(expected) <= TOL, (nd, got, expected)
 
 
+def test_no_alloc_reduce_edge_sizes_and_cleanup():
+    """nd = 0 writes 0; sizes that fill the last 4096-visibility block exactly
+    agree with the regular entry point; a call after galario_cleanup() (which
+    forgets the cached scratch address) looks the address up again."""
+    torch = pytest.importorskip("torch")
+    import galario_gb300 as g
+    g.double.use_gpu(0)
+    L, f = _lib()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    out = torch.full((1,), 7.0, dtype=torch.float64, device=dev)
+    buf = torch.zeros(8, dtype=torch.float64, device=dev)
+    p = buf.data_ptr()
+    assert f(0, p, p, p, p, out.data_ptr(), C.c_void_p(stream.cuda_stream)) == 0, L.galario_last_error()
+    stream.synchronize()
+    assert float(out.item()) == 0.0
+    for nd, seed, cleanup in ((4096, 3, False), (4096 * 5, 4, True), (4096 * 37, 5, False)):
+        if cleanup:
+            assert L.galario_cleanup() == 0
+        re, im, w, vis = _case(nd, seed)
+        expected = g.double.reduce_chi2(re, im, w, vis)
+        t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (re, im, w)]
+        tv = torch.from_numpy(vis.view(np.float64).copy()).to(dev)
+        st = f(nd, t[0].data_ptr(), t[1].data_ptr(), tv.data_ptr(), t[2].data_ptr(), out.data_ptr(),
+               C.c_void_p(stream.cuda_stream))
+        assert st == 0, L.galario_last_error()
+        stream.synchronize()
+        got = float(out.item())
+        assert abs(got - expected) / abs(expected) <= TOL, (nd, got, expected)
+
+
+def test_no_alloc_reduce_rejects_misaligned_vis():
+    """vis_dev is read 16 bytes at a time: a view starting at an odd double is
+    rejected on the host, before anything is enqueued."""
+    torch = pytest.importorskip("torch")
+    L, f = _lib()
+    dev = torch.device("cuda", 0)
+    buf = torch.zeros(64, dtype=torch.float64, device=dev)
+    out = torch.zeros(1, dtype=torch.float64, device=dev)
+    p = buf.data_ptr()
+    assert p % 16 == 0
+    st = f(4, p, p, p + 8, p, out.data_ptr(), None)
+    assert st == 1  # GALARIO_EINVAL
+    assert b"16-byte aligned" in L.galario_last_error()
+
+
 def test_no_alloc_reduce_rejects_sizes_beyond_the_maximum():
     torch = pytest.importorskip("torch")
     L, f = _lib()
