@@ -48,6 +48,7 @@
 #include "../../include/galario_gb300.h"
 #include "gb_device.cuh"
 #include "gb_internal.cuh"
+#include "gb_tune.h"
 
 namespace gbg {
 void set_error_message(const std::string& msg);  // gb_api.cu
@@ -1261,11 +1262,12 @@ __global__ void __launch_bounds__(MAXT) rowsT_image_batch_kernel(Geo g, int F, c
 // launch-shape autotuner: per geometry, each pass's candidate shapes (complex
 // values per thread of the FFT passes, visibilities per thread of the vis pass)
 // are timed once with CUDA events on the caller's stream and the fastest is
-// cached.  GALARIO_AUTOTUNE=0 keeps the default shapes.
+// kept, in memory and in the cache file of gb_tune.h (keyed by GPU name,
+// geometry, batch size and visibility-count bucket), so a later process on
+// the same kind of GPU skips the timing.  GALARIO_AUTOTUNE=0 keeps the
+// default shapes.
 // ---------------------------------------------------------------------------
-struct Shape {
-    int e_rows, e_cols, e_colsT, e_rowsT, pts;
-};
+using Shape = tune::Shape;
 struct TuneKey {
     int N, K, W, R, B, nd, grad, nr, image;
     bool operator<(const TuneKey& o) const {
@@ -1287,6 +1289,18 @@ Shape default_shape(const Geo& g) {
     sh.pts = 4;
     return sh;
 }
+// a cached shape is used only if every field is one of the current candidates
+bool shape_valid(const Geo& g, const Shape& sh, bool real, bool tma_ok) {
+    auto in = [](int x, const std::vector<int>& c) {
+        for (int y : c)
+            if (y == x) return true;
+        return false;
+    };
+    const std::vector<int> rows = fft_candidates(g.M), cols = fft_candidates(g.N);
+    const bool col_ok = in(sh.e_cols, cols) || (tma_ok && sh.e_cols >= kTmaCols && in(sh.e_cols - kTmaCols, cols));
+    const std::vector<int> pts = real ? std::vector<int>{2, 4, 8} : std::vector<int>{2, 4};
+    return in(sh.e_rows, rows) && col_ok && in(sh.e_colsT, cols) && in(sh.e_rowsT, rows) && in(sh.pts, pts);
+}
 bool graphs_enabled() {
     const char* v = std::getenv("GALARIO_GRAPHS");
     return !(v && v[0] == '0');
@@ -1307,29 +1321,32 @@ struct Tuner {
         cudaEventDestroy(b);
     }
     // every candidate: one warm-up launch, then the fastest of three timed
-    // launches, the candidates interleaved so that clock or cache drift
-    // between them does not decide
+    // launches (tune::best_of), timed with CUDA events on the caller's stream
     template <class F> int best(const std::vector<int>& cand, F&& run) {
-        if (cand.empty()) return 8;
-        std::vector<float> best_ms(cand.size(), 1e30f);
-        for (int c : cand) run(c);
-        for (int rep = 0; rep < 3; ++rep) {
-            for (size_t i = 0; i < cand.size(); ++i) {
-                cudaEventRecord(a, s);
-                run(cand[i]);
-                cudaEventRecord(b, s);
-                if (cudaEventSynchronize(b) != cudaSuccess) return cand[0];
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, a, b);
-                best_ms[i] = std::min(best_ms[i], ms);
-            }
-        }
-        size_t k = 0;
-        for (size_t i = 1; i < cand.size(); ++i)
-            if (best_ms[i] < best_ms[k]) k = i;
-        return cand[k];
+        return tune::best_of(cand, run, [&](int c) -> double {
+            cudaEventRecord(a, s);
+            run(c);
+            cudaEventRecord(b, s);
+            if (cudaEventSynchronize(b) != cudaSuccess) return -1.0;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            return ms;
+        });
     }
 };
+
+// the tuning cache file, shared by every device of the process
+tune::Cache& tune_file() {
+    static tune::Cache c(tune::default_path());
+    return c;
+}
+tune::Key tune_file_key(int N, int K, int W, int R, int B, long long nd_pad, int grad, int nr, int image) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp prop;
+    const char* name = cudaGetDeviceProperties(&prop, dev) == cudaSuccess ? prop.name : "unknown";
+    return tune::Key{tune::gpu_token(name), N, K, W, R, B, tune::nvis_bucket(nd_pad), grad, nr, image};
+}
 
 struct Err {
     int status;
@@ -2087,8 +2104,17 @@ static void batch_run(const BatchCall& call) {
         const TuneKey key{g.N, g.K, g.W, g.R, B, d->nd_pad, grad ? 1 : 0, nr, image ? 1 : 0};
         auto it = ws.shapes.find(key);
         const bool tuned = it != ws.shapes.end();
+        tune::Key fkey;
+        Shape fsh;
+        const bool from_file = !tuned && autotune_enabled() &&
+                               (fkey = tune_file_key(g.N, g.K, g.W, g.R, B, d->nd_pad, grad ? 1 : 0, nr, image ? 1 : 0),
+                                tune_file().lookup(fkey, &fsh)) &&
+                               shape_valid(g, fsh, real, tma_ok);
         if (tuned) {
             sh = it->second;
+        } else if (from_file) {
+            sh = fsh;
+            ws.shapes[key] = sh;
         } else if (autotune_enabled()) {
             Tuner tu(s);
             std::vector<int> col_shapes = fft_candidates(g.N);
@@ -2107,6 +2133,7 @@ static void batch_run(const BatchCall& call) {
                 sh.e_rowsT = tu.best(fft_candidates(g.M), [&](int e) { sh.e_rowsT = e; run_all(); });
             }
             ws.shapes[key] = sh;
+            tune_file().store(fkey, sh);
         }
 
         // First call of a combination: eager (it also sets the kernels'
