@@ -136,6 +136,72 @@ def algorithmic_bytes(wl: Workload, s: int):
 
 
 # ---------------------------------------------------------------------------
+# the large single-model image workload: chi2Image, nxy=8192, dxy=1.5e-3",
+# three Gaussian rings (r0 0.2"/0.5"/0.9", sigma 0.03"/0.05"/0.08") and a
+# Gaussian blob (sigma 0.02") at a seeded position within 0.5" of the centre,
+# the four of equal flux, 0.1 Jy in total; Nvis=1e7 with radius log-uniform in
+# [1e4, 1.5e7] wavelengths; noise as above; dRA=0.05", dDec=-0.03", PA=0;
+# seed 2.  Synthetic.
+# ---------------------------------------------------------------------------
+class ImageWorkload:
+    nxy = 8192
+    dxy = 1.5e-3 * ARCSEC
+    nd = 10_000_000
+
+    def __init__(self, seed=2):
+        rng = np.random.default_rng(seed)
+        N = self.nxy
+        x = (np.arange(N) - N / 2) * self.dxy
+        r2 = x[None, :] ** 2 + x[:, None] ** 2
+        rad = np.sqrt(r2)
+        img = np.zeros((N, N))
+        for r0, sig in ((0.2, 0.03), (0.5, 0.05), (0.9, 0.08)):
+            ring = np.exp(-0.5 * ((rad - r0 * ARCSEC) / (sig * ARCSEC)) ** 2)
+            img += ring * (0.025 / ring.sum())
+        del rad
+        rb, tb = 0.5 * np.sqrt(rng.uniform()) * ARCSEC, rng.uniform(0, 2 * np.pi)
+        bx, by = rb * np.cos(tb), rb * np.sin(tb)
+        blob = np.exp(-0.5 * ((x[None, :] - bx) ** 2 + (x[:, None] - by) ** 2) / (0.02 * ARCSEC) ** 2)
+        img += blob * (0.025 / blob.sum())
+        del blob, r2
+        self.image = img
+        r = np.exp(rng.uniform(np.log(1e4), np.log(1.5e7), self.nd))
+        th = rng.uniform(0, 2 * np.pi, self.nd)
+        self.u, self.v = r * np.cos(th), r * np.sin(th)
+        sigma = rng.uniform(0.5e-3, 1.5e-3, self.nd)
+        self.noise_re = rng.normal(0, sigma)
+        self.noise_im = rng.normal(0, sigma)
+        self.w = 1. / sigma ** 2
+
+    @property
+    def duv(self):
+        return 1. / (self.dxy * self.nxy)
+
+    def kw(self):
+        return dict(dRA=0.05 * ARCSEC, dDec=-0.03 * ARCSEC, PA=0.0)
+
+    def describe(self):
+        return ("chi2Image nxy=8192 dxy=1.5e-3\" 3 rings + blob, Nvis=1e7 radius log-uniform [1e4, 1.5e7] "
+                "(config 2), device-resident inputs, L2 flushed between steps")
+
+    def algorithmic_bytes(self, s: int):
+        """Algorithmic HBM bytes per launch of each kernel, s = bytes per real."""
+        N, nd = self.nxy, self.nd
+        ext = np.sqrt(np.max(self.u ** 2 + self.v ** 2)) / self.duv * (1 + 2e-6) + 1e-6
+        K = min(N // 2 + 1, int(np.floor(ext)) + 2)
+        kv = int(np.ceil(ext))
+        r0, r1 = max(0, N // 2 - kv - 1), min(N, N // 2 + kv + 3)
+        W = r1 - r0
+        return {
+            "extent": nd * 2 * s,                        # read u, v
+            "rows": N * N * s + N * K * 2 * s,           # read the image, write N x K complex
+            "cols": K * N * 2 * s + K * W * 3 * s,       # read K columns, write window + moduli
+            "quad": K * W * 3 * s + K * W * 16 * s,      # read window + moduli, write cell records
+            "vis": nd * 5 * s,                           # read u, v, Re, Im, w (gathers hit L2)
+        }, {"K": K, "W": W, "R_rows": N}
+
+
+# ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
 class ClockSampler:
@@ -176,10 +242,13 @@ class ClockSampler:
             self.proc = None
 
     def summary(self):
+        """Median SM clock and throttle reasons over the timed regions.  A
+        region shorter than the sampling interval may hold no sample: it then
+        takes the nearest sample within 0.25 s of it (the clock a few ms away
+        from a region that ran at full load)."""
         if not self.out:
             return None
-        import datetime
-        sm, mx, reasons = [], [], set()
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for row in csv.reader(io.StringIO(self.out)):
             if len(row) < 10:
@@ -189,17 +258,31 @@ class ClockSampler:
                 clk, cmax = float(row[2]), float(row[3])
             except ValueError:
                 continue
-            if not any(a <= ts <= b for a, b in self.windows):
-                continue
-            sm.append(clk)
-            mx.append(cmax)
-            for n, val in zip(names, row[6:10]):
-                if val.strip().lower() == "active":
-                    reasons.add(n)
-        if not sm:
+            act = [n for n, val in zip(names, row[6:10]) if val.strip().lower() == "active"]
+            rows.append((ts, clk, cmax, act))
+        if not rows:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
-                "reasons": sorted(reasons), "regions": "the timed loops of the FP64, FP32 and end-to-end rates"}
+        picked, inside, nearest = {}, 0, 0
+        for a, b in self.windows:
+            got = [i for i, r in enumerate(rows) if a <= r[0] <= b]
+            if got:
+                inside += len(got)
+            else:
+                mid = a + (b - a) / 2
+                i = min(range(len(rows)), key=lambda j: abs((rows[j][0] - mid).total_seconds()))
+                if abs((rows[i][0] - mid).total_seconds()) <= 0.25 + (b - a).total_seconds() / 2:
+                    got = [i]
+                    nearest += 1
+            for i in got:
+                picked[i] = rows[i]
+        if not picked:
+            return None
+        sel = list(picked.values())
+        return {"sm_mhz": statistics.median(r[1] for r in sel), "sm_max_mhz": max(r[2] for r in sel),
+                "sm_mhz_min": min(r[1] for r in sel), "samples": len(sel), "samples_inside": inside,
+                "regions_nearest_sample": nearest, "regions": len(self.windows),
+                "reasons": sorted({n for r in sel for n in r[3]}),
+                "how": "nvidia-smi every 20 ms; samples inside the timed loops (all legs), or the nearest one"}
 
 
 def profiled_traffic(stage: str, precision: str):
@@ -222,6 +305,27 @@ def peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def profiled_fp64_work(kernel: str):
+    """(FP64 flops, FP64-pipe thread instructions) per visibility of a kernel
+    from the committed ncu summary (flops = 2 DFMA + DADD + DMUL; the pipe
+    count adds conversions and compares), or None."""
+    p = os.path.join(ROOT, "profiles", "fp64_work.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) == 3 and not line.startswith("#") and parts[0] == kernel:
+                return float(parts[1]), float(parts[2])
+    return None
+
+
+def step_stats(ms):
+    """Per-step times (ms) of a timed loop: mean, median, min, max."""
+    return {"ms_mean": sum(ms) / len(ms), "ms_median": statistics.median(ms), "ms_min": min(ms),
+            "ms_max": max(ms), "steps": len(ms)}
 
 
 # ---------------------------------------------------------------------------
@@ -297,9 +401,7 @@ def run_ours(args):
     wl = Workload(seed=0)
     L = _lib.lib()
     dev = torch.device("cuda", local)
-    clock_sampler = ClockSampler(local)
-    if args.part == "all":
-        clock_sampler.start()
+    clock_sampler = ClockSampler(local).start()
     # a dedicated stream: the library's kernels, the L2 flush and the timing
     # events are all ordered on it
     stream = torch.cuda.Stream(dev)
@@ -314,6 +416,48 @@ def run_ours(args):
         return torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dt)
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def timed(fn, steps, barrier=False):
+        """W warm-up calls, then `steps` calls each bracketed by CUDA events on
+        the library's stream, the L2 flush between them outside the events.
+        Returns the per-step milliseconds and the last output."""
+        out = None
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                flush.zero_()
+                out = fn()
+            torch.cuda.synchronize()
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            if barrier and dist is not None:
+                dist.barrier()
+            torch.cuda.synchronize()
+            d0 = datetime.datetime.now()
+            for a, b in evs:
+                flush.zero_()
+                a.record(stream)
+                out = fn()
+                b.record(stream)
+            torch.cuda.synchronize()
+            clock_sampler.mark(d0, datetime.datetime.now())
+        if barrier and dist is not None:
+            dist.barrier()
+        return [a.elapsed_time(b) for a, b in evs], out
+
+    def stage_times_begin():
+        _lib.check(L.galario_stage_timing(1))
+        _lib.check(L.galario_stage_times((C.c_double * 8)(), (C.c_int * 8)(), 8))  # discard earlier records
+
+    def stage_times_end():
+        ms_sum = (C.c_double * 8)()
+        cnt = (C.c_int * 8)()
+        _lib.check(L.galario_stage_times(ms_sum, cnt, 8))
+        _lib.check(L.galario_stage_timing(0))
+        err = C.c_uint(0)
+        _lib.check(L.galario_device_status(C.byref(err)))
+        if err.value:
+            raise RuntimeError("device error bits %d" % err.value)
+        return {L.galario_stage_name(i).decode(): (ms_sum[i] / cnt[i] if cnt[i] else 0.0) for i in range(8)
+                if cnt[i]}
 
     def device_rate(precision):
         dt = torch.float64 if precision == "double" else torch.float32
@@ -332,55 +476,73 @@ def run_ours(args):
         def step():
             _lib.check(fn(*cargs))
 
+        for _ in range(args.warmup):
+            step()
         torch.cuda.synchronize()
-        with torch.cuda.stream(stream):
-            for _ in range(args.warmup):
-                flush.zero_()
-                step()
-        torch.cuda.synchronize()
-        _lib.check(L.galario_stage_timing(1))
-        _lib.check(L.galario_stage_times((C.c_double * 8)(), (C.c_int * 8)(), 8))  # discard warm-up records
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
-        with torch.cuda.stream(stream):
-            d0 = datetime.datetime.now()
-            t0 = time.perf_counter()
-            for a, b in evs:
-                flush.zero_()
-                a.record(stream)
-                step()
-                b.record(stream)
-            torch.cuda.synchronize()
-            wall = time.perf_counter() - t0
-            clock_sampler.mark(d0, datetime.datetime.now())
-        if dist is not None:
-            dist.barrier()
-        ms = sum(a.elapsed_time(b) for a, b in evs)
-        ms_sum = (C.c_double * 8)()
-        cnt = (C.c_int * 8)()
-        _lib.check(L.galario_stage_times(ms_sum, cnt, 8))
-        _lib.check(L.galario_stage_timing(0))
-        err = C.c_uint(0)
-        _lib.check(L.galario_device_status(C.byref(err)))
-        if err.value:
-            raise RuntimeError("device error bits %d" % err.value)
-        stages = {L.galario_stage_name(i).decode(): (ms_sum[i] / cnt[i] if cnt[i] else 0.0) for i in range(8)
-                  if cnt[i]}
-        return ms, stages, float(chi2_d.item()), None, wall
+        stage_times_begin()
+        ms, _ = timed(step, args.steps, barrier=True)
+        stages = stage_times_end()
+        return ms, stages, float(chi2_d.item())
 
     if args.part == "batched":  # profiling runs of the batched path: the FP64 chi2 from one public call
         chi2_64 = g.double.chi2Profile(wl.intensity, wl.Rmin, wl.dR, wl.nxy, wl.dxy, wl.u, wl.v, re, im, wl.w,
                                        **wl.kw())
-    else:
-        ms64, stages64, chi2_64, clocks, wall64 = device_rate("double")
-        ms32, stages32, chi2_32, _, _ = device_rate("single")
+    elif args.part in ("all", "plain"):
+        ms64_l, stages64, chi2_64 = device_rate("double")
+        ms32_l, stages32, chi2_32 = device_rate("single")
+        ms64, ms32 = sum(ms64_l), sum(ms32_l)
     if args.part == "plain":
         if rank == 0:
             print(json.dumps({"part": "plain", "f64_evals_per_s": world * args.steps / (ms64 / 1e3),
                               "f32_evals_per_s": world * args.steps / (ms32 / 1e3), "stages_f64": stages64,
-                              "stages_f32": stages32}), flush=True)
+                              "stages_f32": stages32, "f64_steps": step_stats(ms64_l),
+                              "f32_steps": step_stats(ms32_l)}), flush=True)
+        return 0
+
+    # the large single-model image workload (chi2Image, nxy=8192, 1e7
+    # visibilities), FP64 and FP32, with per-kernel times and HBM GB/s
+    def image8192():
+        iw = ImageWorkload()
+        model = g.double.sampleImage(iw.image, iw.dxy, iw.u, iw.v, **iw.kw())
+        ire, iim = model.real + iw.noise_re, model.imag + iw.noise_im
+        del model
+        out = {"workload": iw.describe(), "steps": max(20, min(args.steps, 50))}
+        for precision, s in (("double", 8), ("single", 4)):
+            dt = torch.float64 if precision == "double" else torch.float32
+            R = C.c_double if precision == "double" else C.c_float
+            img_d = to_dev(iw.image, dt)
+            u_d, v_d, re_d, im_d, w_d = (to_dev(x, dt) for x in (iw.u, iw.v, ire, iim, iw.w))
+            chi2_d = torch.zeros(1, dtype=torch.float64, device=dev)
+            fn = _lib.fn("chi2_image_device", precision)
+            kw = iw.kw()
+            cargs = (iw.nxy, iw.nxy, img_d.data_ptr(), R(1.0), R(kw["dRA"]), R(kw["dDec"]), R(iw.duv), R(kw["PA"]),
+                     iw.nd, u_d.data_ptr(), v_d.data_ptr(), re_d.data_ptr(), im_d.data_ptr(), w_d.data_ptr(),
+                     chi2_d.data_ptr(), sptr)
+
+            def step():
+                _lib.check(fn(*cargs))
+
+            step()
+            torch.cuda.synchronize()
+            stage_times_begin()
+            ms, _ = timed(step, out["steps"])
+            stages = stage_times_end()
+            alg, win = iw.algorithmic_bytes(s)
+            per = {}
+            for k, t in stages.items():
+                if k in alg:
+                    per[k] = {"ms": round(t, 4), "bytes": alg[k], "GBs": alg[k] / (t * 1e-3) / 1e9,
+                              "hbm_frac": alg[k] / (t * 1e-3) / 1e9 / peaks()[0]}
+            out["f64" if s == 8 else "f32"] = dict(
+                {"evals_per_s": len(ms) / (sum(ms) / 1e3), "chi2": float(chi2_d.item()), "kernels": per}, **step_stats(ms))
+            out["window"] = win
+            del img_d, u_d, v_d, re_d, im_d, w_d
+        out["rel_chi2_f32_vs_f64"] = abs(out["f32"]["chi2"] - out["f64"]["chi2"]) / abs(out["f64"]["chi2"])
+        return out
+
+    if args.part == "image8192":
+        if rank == 0:
+            print(json.dumps({"part": "image8192", "image8192": image8192()}), flush=True)
         return 0
 
     # batched FP32 + gradient: B models (model 0 = the workload's parameters,
@@ -400,26 +562,26 @@ def run_ours(args):
         scale = 1 + np.r_[0, rng.uniform(-0.1, 0.1, B - 1)]
         tI = torch.tensor(np.outer(scale, wl.intensity), dtype=torch.float32, device=dev)
         tp = torch.tensor(prm, dtype=torch.float32, device=dev)
-        steps = max(3, args.steps // 10)
-        with torch.cuda.stream(stream):
-            for _ in range(args.warmup):
-                flush.zero_()
-                out = chi2_profile_batch(ds, tI, tp, wl.Rmin, wl.dR, wl.dxy, wl.nxy, grad=True)
-            torch.cuda.synchronize()
-            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-            for a, b in evs:
-                flush.zero_()
-                a.record(stream)
-                out = chi2_profile_batch(ds, tI, tp, wl.Rmin, wl.dR, wl.dxy, wl.nxy, grad=True)
-                b.record(stream)
-            torch.cuda.synchronize()
-        ms = sum(a.elapsed_time(b) for a, b in evs)
-        chi2_b0 = float(out[0][0].item())
+        ms, out = timed(lambda: chi2_profile_batch(ds, tI, tp, wl.Rmin, wl.dR, wl.dxy, wl.nxy, grad=True),
+                        max(20, args.steps))
+        chi2_b = out[0].double().cpu().numpy()
         ds.close()
-        return {"value": B * steps / (ms * 1e-3), "unit": UNIT, "B": B, "steps": steps, "dtype": "f32",
-                "gradient": "chi2 and dchi2/d(4096 profile samples, inc, PA, dRA, dDec) per model",
-                "ms_per_step": ms / steps, "rel_chi2_vs_f64": abs(chi2_b0 - chi2_64) / abs(chi2_64),
-                "gpu_launches_per_step": 10}
+        # every model's FP32 chi2 against the FP64 module on the same inputs:
+        # the dataset (stored as float32), the profiles, parameters and
+        # geometry rounded to float32 as the batched call receives them
+        prm32, I32 = tp.double().cpu().numpy(), tI.double().cpu().numpy()
+        f32 = lambda a: np.asarray(a, dtype=np.float32).astype(np.float64)  # noqa: E731
+        u32, v32, re32, im32, w32 = (f32(x) for x in (wl.u, wl.v, re, im, wl.w))
+        Rmin32, dR32, dxy32 = (float(np.float32(x)) for x in (wl.Rmin, wl.dR, wl.dxy))
+        rel = 0.0
+        for b in range(B):
+            ref = g.double.chi2Profile(I32[b], Rmin32, dR32, wl.nxy, dxy32, u32, v32, re32, im32, w32,
+                                       inc=prm32[b, 0], PA=prm32[b, 1], dRA=prm32[b, 2], dDec=prm32[b, 3])
+            rel = max(rel, abs(chi2_b[b] - ref) / abs(ref))
+        return dict({"value": B * len(ms) / (sum(ms) * 1e-3), "unit": UNIT, "B": B, "dtype": "f32",
+                     "gradient": "chi2 and dchi2/d(4096 profile samples, inc, PA, dRA, dDec) per model",
+                     "ms_per_step": sum(ms) / len(ms), "max_rel_chi2_vs_f64_all_models": rel,
+                     "gpu_launches_per_step": 10}, **step_stats(ms))
 
     # the multi-dataset workload: B single-ring profiles, nxy=2048, dxy=5e-3",
     # Rmin=1e-4", dR=4e-4", nr=4096; 8 visibility sets with nd_k ~ U[2e5, 3e6],
@@ -435,21 +597,6 @@ def run_ours(args):
             sets.append((rad * np.cos(th), rad * np.sin(th), r.normal(0, sig), r.normal(0, sig), 1 / sig ** 2))
         return sets
 
-    def timed(fn, steps):
-        with torch.cuda.stream(stream):
-            for _ in range(args.warmup):
-                flush.zero_()
-                out = fn()
-            torch.cuda.synchronize()
-            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-            for a, b in evs:
-                flush.zero_()
-                a.record(stream)
-                out = fn()
-                b.record(stream)
-            torch.cuda.synchronize()
-        return sum(a.elapsed_time(b) for a, b in evs), out
-
     def batched_sets_rate(ds, B=256):
         from galario_gb300.batch import chi2_profile_batch
         nxy, dxy, Rmin, dR, nr = 2048, 5e-3 * ARCSEC, 1e-4 * ARCSEC, 4e-4 * ARCSEC, 4096
@@ -462,12 +609,12 @@ def run_ours(args):
         prm = np.c_[r.uniform(0, 70, B) * DEG, r.uniform(0, 180, B) * DEG, np.zeros(B), np.zeros(B)]
         tI = torch.tensor(prof, dtype=torch.float32, device=dev)
         tp = torch.tensor(prm, dtype=torch.float32, device=dev)
-        steps = max(3, args.steps // 60)
-        out = {"B": B, "nsets": ds.nsets, "nvis": ds.nd, "nxy": nxy, "steps": steps, "unit": UNIT}
+        out = {"B": B, "nsets": ds.nsets, "nvis": ds.nd, "nxy": nxy, "unit": UNIT}
         for grad in (False, True):
             ms, _ = timed(lambda: chi2_profile_batch(ds, tI, tp, Rmin, dR, dxy, nxy, grad=grad, per_set=True),
-                          steps)
-            out["grad" if grad else "forward"] = {"value": B * steps / (ms * 1e-3), "ms_per_step": ms / steps}
+                          max(20, min(args.steps, 40)))
+            out["grad" if grad else "forward"] = dict({"value": B * len(ms) / (sum(ms) * 1e-3),
+                                                       "ms_per_step": sum(ms) / len(ms)}, **step_stats(ms))
         return out
 
     def batched_images_rate(ds, B=16):
@@ -484,11 +631,10 @@ def run_ours(args):
             imgs[b] = torch.from_numpy(ring * (0.1 / ring.sum()))
         tp = torch.tensor(np.c_[r.uniform(0, np.pi, B), r.uniform(-0.05, 0.05, (B, 2)) * ARCSEC],
                           dtype=torch.float32, device=dev)
-        steps = max(3, args.steps // 60)
-        ms, _ = timed(lambda: chi2_image_batch(ds, imgs, tp, dxy, grad=True), steps)
-        return {"value": B * steps / (ms * 1e-3), "unit": UNIT, "B": B, "nxy": nxy, "nsets": ds.nsets,
-                "nvis": ds.nd, "ms_per_step": ms / steps, "steps": steps,
-                "gradient": "chi2 and dchi2/d(every pixel, PA, dRA, dDec) per image"}
+        ms, _ = timed(lambda: chi2_image_batch(ds, imgs, tp, dxy, grad=True), max(20, min(args.steps, 40)))
+        return dict({"value": B * len(ms) / (sum(ms) * 1e-3), "unit": UNIT, "B": B, "nxy": nxy, "nsets": ds.nsets,
+                     "nvis": ds.nd, "ms_per_step": sum(ms) / len(ms),
+                     "gradient": "chi2 and dchi2/d(every pixel, PA, dRA, dDec) per image"}, **step_stats(ms))
 
     batched = batched_rate()
     from galario_gb300.batch import Dataset as _Dataset
@@ -503,6 +649,7 @@ def run_ours(args):
             print(json.dumps({"part": "batched", "batched": batched, "batched_sets": batched_sets,
                               "batched_images": batched_images}), flush=True)
         return 0
+    img8192 = image8192()
 
     # max over ranks of the timed region
     t_local = ms64 / 1e3
@@ -512,12 +659,34 @@ def run_ours(args):
         t_local = float(t.item())
     value = world * args.steps / t_local
 
-    # e2e: public API, pinned host inputs, H2D + D2H inside every step
+    # e2e: public API, host inputs, H2D + D2H inside every step; pinned
+    # (page-locked) host arrays, and plain (pageable) numpy arrays as a
+    # drop-in caller passes them
     def pinned(a, dt):
         t = torch.empty(len(a), dtype=dt, pin_memory=True)
         arr = t.numpy()
         arr[:] = a
         return t, arr
+
+    def e2e_rate(host):
+        chi2 = None
+        for _ in range(max(1, min(args.warmup, 3))):
+            chi2 = g.double.chi2Profile(host["I"], wl.Rmin, wl.dR, wl.nxy, wl.dxy, host["u"], host["v"], host["re"],
+                                        host["im"], host["w"], **wl.kw())
+        if dist is not None:
+            dist.barrier()
+        d0 = datetime.datetime.now()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            chi2 = g.double.chi2Profile(host["I"], wl.Rmin, wl.dR, wl.nxy, wl.dxy, host["u"], host["v"],
+                                        host["re"], host["im"], host["w"], **wl.kw())
+        dt = time.perf_counter() - t0
+        clock_sampler.mark(d0, datetime.datetime.now())
+        if dist is not None:
+            t = torch.tensor([dt], dtype=torch.float64, device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        return world * args.steps / dt, chi2
 
     keep = []
     host = {}
@@ -525,27 +694,10 @@ def run_ours(args):
         t, arr = pinned(a, torch.float64)
         keep.append(t)
         host[name] = arr
-    e2e_chi2 = None
-    for _ in range(max(1, min(args.warmup, 3))):
-        e2e_chi2 = g.double.chi2Profile(host["I"], wl.Rmin, wl.dR, wl.nxy, wl.dxy, host["u"], host["v"], host["re"],
-                                        host["im"], host["w"], **wl.kw())
-    e2e_steps = args.steps
-    if dist is not None:
-        dist.barrier()
-    d0 = datetime.datetime.now()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_chi2 = g.double.chi2Profile(host["I"], wl.Rmin, wl.dR, wl.nxy, wl.dxy, host["u"], host["v"],
-                                        host["re"], host["im"], host["w"], **wl.kw())
-    e2e_t = time.perf_counter() - t0
-    clock_sampler.mark(d0, datetime.datetime.now())
+    e2e_value, e2e_chi2 = e2e_rate(host)
+    e2e_pageable, _ = e2e_rate({"I": wl.intensity, "u": wl.u, "v": wl.v, "re": re, "im": im, "w": wl.w})
     clock_sampler.stop()
     clocks = clock_sampler.summary()
-    if dist is not None:
-        t = torch.tensor([e2e_t], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_t = float(t.item())
-    e2e_value = world * e2e_steps / e2e_t
     h2d_bytes = 8 * (wl.nr + 5 * wl.nd)
     d2h_bytes = 64  # device state block carrying chi2 and the error bits
 
@@ -555,24 +707,43 @@ def run_ours(args):
         alg, win = algorithmic_bytes(wl, 8)
         dom = max((k for k in stages64 if k in alg), key=lambda k: stages64[k])
         achieved = alg[dom] / (stages64[dom] * 1e-3) / 1e9
+        fp64_peak = C.c_double(0.0)
+        _lib.check(L.galario_measure_fp64_peak(C.byref(fp64_peak)))
+        work = profiled_fp64_work("vis_kernel_f64_profile") if dom == "vis" else None
         rate_cpu, kind, cores, chi2_cpu, dt_cpu = cpu_chi2_profile_rate(wl, re, im, steps=2)
         alg32, _ = algorithmic_bytes(wl, 4)
+        roof = {"kernel": dom, "algorithmic_bytes": alg[dom],
+                "traffic": profiled_traffic(dom, "f64"),
+                "traffic_source": "profiles/dram_traffic.txt (ncu dram__bytes_read+write of one launch)",
+                "hbm": {"achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                        "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}}
+        if work is not None:
+            # the FP64 pipe binds this kernel: its fraction is the primary one.
+            # achieved = FP64-pipe thread instructions per second (ncu count per
+            # visibility x visibilities / live event time); peak = the measured
+            # FP64 FMA rate in instructions per second (flops / 2)
+            flops_pv, inst_pv = work
+            t = stages64[dom] * 1e-3
+            roof.update({"bound": "fp64", "achieved": inst_pv * wl.nd / t / 1e9, "peak": fp64_peak.value / 2,
+                         "unit": "G FP64-pipe instr/s", "frac": inst_pv * wl.nd / t / 1e9 / (fp64_peak.value / 2),
+                         "fp64_gflops": flops_pv * wl.nd / t / 1e9, "fp64_peak_gflops": fp64_peak.value,
+                         "peak_source": "measured in this run (galario_measure_fp64_peak: FP64 FMA chains)",
+                         "per_vis": {"fp64_flops": flops_pv, "fp64_pipe_instr": inst_pv},
+                         "work_source": "profiles/fp64_work.txt (ncu FP64 thread instructions of one launch "
+                                        "/ visibilities)"})
+        else:
+            roof.update({"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "fp64_peak_gflops": fp64_peak.value})
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms64 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": wl.config(),
+            "step_stats": step_stats(ms64_l),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes,
-                    "d2h_bytes_per_step": d2h_bytes, "api": "galario_gb300.double.chi2Profile, pinned numpy inputs"},
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-                         "traffic": profiled_traffic(dom, "f64"), "algorithmic_bytes": alg[dom],
-                         "traffic_source": "profiles/dram_traffic.txt (ncu dram__bytes_read+write of one launch)",
-                         "note": "FP64 arithmetic on GB300 runs at ~1.2 TFLOP/s; the FP64 kernels are "
-                                 "FP64-issue-bound, not HBM-bound",
-                         "fp64_pipe_active": 0.852,
-                         "fp64_pipe_source": "profiles/vis_kernel_f64_chi2Profile_nxy4096_nvis2M.md "
-                                             "(ncu sm__pipe_fp64_cycles_active of the vis kernel)"},
+                    "d2h_bytes_per_step": d2h_bytes, "api": "galario_gb300.double.chi2Profile, pinned numpy inputs",
+                    "pageable": {"value": e2e_pageable, "api": "the same call with plain (pageable) numpy inputs"}},
+            "roofline": roof,
             "stages_ms": {k: round(v, 4) for k, v in stages64.items()},
             "window": win,
             "single": {"value": world * args.steps / (ms32 / 1e3), "unit": UNIT, "dtype": "f32",
@@ -582,6 +753,7 @@ def run_ours(args):
             "batched": dict(batched, ratio_vs_plain_f64=batched["value"] / value),
             "batched_sets": batched_sets,
             "batched_images": batched_images,
+            "image8192": img8192,
             "cpu_baseline": {"value": rate_cpu, "unit": UNIT, "cores": cores, "kind": kind,
                              "sample": "2 full chi2Profile evaluations (FP64, FFT from the project's C FFT in place "
                                        "of FFTW), first call dropped"},
@@ -604,7 +776,7 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--part", choices=["all", "plain", "batched"], default="all")
+    ap.add_argument("--part", choices=["all", "plain", "batched", "image8192"], default="all")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -75,8 +75,9 @@ def lib() -> C.CDLL:
         L.galario_stage_name.argtypes = [_i]
         L.galario_stage_name.restype = C.c_char_p
         L.galario_stage_times.argtypes = [C.POINTER(C.c_double), C.POINTER(_i), _i]
+        L.galario_measure_fp64_peak.argtypes = [C.POINTER(C.c_double)]
         for n in ("galario_ngpus", "galario_use_gpu", "galario_init", "galario_cleanup", "galario_device_status",
-                  "galario_stage_timing", "galario_stage_times"):
+                  "galario_stage_timing", "galario_stage_times", "galario_measure_fp64_peak"):
             getattr(L, n).restype = _i
         _lib = L
         return L
