@@ -65,15 +65,9 @@ def test_config_profile_4096_2M(profile_case, oracle_port):
     vis_r = orc.sampleProfile(d(r["I"]), float(geo["Rmin"]), float(geo["dR"]), wl.nxy, float(geo["dxy"]), d(r["u"]),
                               d(r["v"]), **{k: float(x) for k, x in kw32.items()})
     vis32 = g.single.sampleProfile(r["I"], geo["Rmin"], geo["dR"], wl.nxy, geo["dxy"], r["u"], r["v"], **kw32)
-    # The reference interpolates modulus and argument separately: V = A z/|z|
-    # with A the bilinear modulus and z the complex bilinear interpolant.
-    # Where the four corners nearly cancel (|z| << A) the direction z/|z| is
-    # ill-conditioned and an FP32 FFT's rounding (~1e-7 of the spectrum's
-    # norm) is amplified by A/|z|.  So the single bound holds for all but a
-    # handful of such visibilities; the worst is bounded at 1e-4.
+    # every visibility within the single tolerance (measured worst: 3.1e-7)
     err = np.abs(vis32 - vis_r) / np.abs(vis_r).max()
-    assert np.quantile(err, 0.9999) <= SP_V, np.quantile(err, 0.9999)
-    assert err.max() <= 10 * SP_V, err.max()
+    assert err.max() <= SP_V, err.max()
     ref_r = orc.chi2Profile(d(r["I"]), float(geo["Rmin"]), float(geo["dR"]), wl.nxy, float(geo["dxy"]), d(r["u"]),
                             d(r["v"]), d(r["re"]), d(r["im"]), d(r["w"]), **{k: float(x) for k, x in kw32.items()})
     got32 = g.single.chi2Profile(r["I"], geo["Rmin"], geo["dR"], wl.nxy, geo["dxy"], r["u"], r["v"], r["re"],

@@ -48,6 +48,12 @@ def sweep_t(I, inc, Rmin, dR, nxy, dxy):
 
 
 def sample_image_t(img, dxy, u, v, PA, dRA, dDec, v_origin=1.):
+    return sample_image_parts_t(img, dxy, u, v, PA, dRA, dDec, v_origin)[0]
+
+
+def sample_image_parts_t(img, dxy, u, v, PA, dRA, dDec, v_origin=1.):
+    """(V, z, max|S|): the visibilities, the complex bilinear interpolant z
+    of each (whose argument gives the phase) and the spectrum's peak modulus."""
     N = img.shape[0]
     S = torch.fft.fftshift(torch.fft.rfft2(torch.fft.fftshift(img)), dim=0)
     c, s = torch.cos(PA), torch.sin(PA)
@@ -70,7 +76,7 @@ def sample_image_t(img, dxy, u, v, PA, dRA, dDec, v_origin=1.):
     dra = dRA * c - dDec * s
     ddec = dRA * s + dDec * c
     phi = 2 * math.pi * (ur * dra + vr * ddec)
-    return U * torch.exp(1j * phi)
+    return U * torch.exp(1j * phi), z, S.abs().max()
 
 
 def chi2_profile_t(I, inc, PA, dRA, dDec, Rmin, dR, nxy, dxy, u, v, re, im, w):
