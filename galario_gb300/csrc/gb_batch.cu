@@ -48,6 +48,7 @@
 #include "../../include/galario_gb300.h"
 #include "gb_device.cuh"
 #include "gb_internal.cuh"
+#include "gb_tc.cuh"
 #include "gb_tune.h"
 
 namespace gbg {
@@ -478,7 +479,12 @@ __device__ __forceinline__ void locate_point(const Geo& g, const ModelConst& m, 
     const DF cv = df_dot2(u, m.sv, v, m.cu);
     p.ur = a.hi;
     p.vr = cv.hi;
-    const bool neg = a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f);
+    // the sign of u' from the pair's rounded sum: df_dot2's pair is not
+    // normalised (|lo| reaches a few ulps of the products, ~1e-5 cells), so
+    // within that distance of u' = 0 the high part alone can have the wrong
+    // sign and the floor below would give -1
+    const float a_sum = __fadd_rn(a.hi, a.lo);
+    const bool neg = a_sum < 0.f || (a_sum == 0.f && a.hi < 0.f);
     const float su = neg ? -1.f : 1.f;
     p.su = su;
     const DF indu = neg ? df_neg(a) : a;
@@ -568,8 +574,10 @@ __device__ __forceinline__ float real_point(const Geo& g, const ModelConst& m, c
     // rotated coordinates in grid units: a = u'/duv, c = v'/duv
     const DF a = df_dot2(u, m.cu, -v, m.sv);
     const DF cv = df_dot2(u, m.sv, v, m.cu);
-    // u' < 0 reads the Hermitian point (-u', -v'); a real spectrum is unchanged by it
-    const bool neg = a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f);
+    // u' < 0 reads the Hermitian point (-u', -v'); a real spectrum is unchanged
+    // by it.  The sign comes from the pair's rounded sum (see locate_point).
+    const float a_sum = __fadd_rn(a.hi, a.lo);
+    const bool neg = a_sum < 0.f || (a_sum == 0.f && a.hi < 0.f);
     const DF indu = neg ? df_neg(a) : a;
     const float cs = neg ? -cv.hi : cv.hi, cl = neg ? -cv.lo : cv.lo;
     const float vh = __fadd_rn(g.half_nrow, cs);  // N/2 + c: Fast2Sum (|c| < N/2)
@@ -1138,6 +1146,138 @@ __global__ void __launch_bounds__(MAXT, (MAXT <= 256 ? 3 : 1)) rowsT_batch_kerne
     if (threadIdx.x == 0) atomicAdd(&ginc[b], sinc);
 }
 
+// ---------------------------------------------------------------------------
+// Spectrum passes of swept profiles as products with fixed cosine matrices,
+// on the tensor cores (gb_tc.cuh).  The swept image is even in x and y about
+// the centre pixel, so with F[a][c] its folded quadrant (a = |y|, c = |x| in
+// pixels, 0 <= a, c <= rmax; F[0][0] the central pixel) the shifted spectrum
+// is real and
+//     S[r][k] = sum_a Cv[r][a] sum_c Ck[k][c] F[a][c],
+//     Ck[k][c] = w_c cos(2 pi c k / N),  Cv[q][a] = w_a cos(2 pi a |r0 + q - N/2| / N)
+// (w_j = 1 for j = 0 and j = N/2, 2 otherwise: the number of mirror pixels),
+// the reference's fftshift_axis0(rfft2(fftshift(image))) without any sign
+// folding.  For B models the cosine matrices are shared, so the row and the
+// column pass are two batched products per direction:
+//     forward   D1_b = Ck F_b^T        (K x (rmax+1))
+//               S_b  = D1_b Cv^T       (K x W, the window, column-major by k)
+//     adjoint   G1_b = Cv^T G_b^T      ((rmax+1) x K, G_b the window gradient)
+//               GF_b = G1_b Ck         ((rmax+1) x (rmax+1) = dchi2/dF)
+// each FP32 operand as a TF32 hi/lo pair (3xTF32).
+// ---------------------------------------------------------------------------
+// the folded quadrant of every model as a TF32 pair; grid (ceil((rmax+1)^2 / 256), B)
+__global__ void sweep_fold_kernel(Geo g, const float* __restrict__ intensity, const ModelConst* __restrict__ mc,
+                                  float* __restrict__ fhi, float* __restrict__ flo, int ldF) {
+    const int b = blockIdx.y;
+    const int n = g.rmax + 1;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n * n) return;
+    const int a = e / n, c = e - a * n;
+    const ModelConst& m = mc[b];
+    const int off = g.N / 2 - g.rmax;
+    float x;
+    if (a == 0 && c == 0) {
+        x = m.central;
+    } else {
+        x = sweep_pixel<float>(off + g.rmax - a, off + g.rmax - c, intensity + (size_t)b * g.nr, g.nr, g.Rmin, g.dR,
+                               g.inv_dR, g.dxy, m.inv_cos_inc, g.rmax, off, g.sr_to_px);
+    }
+    const float hi = tc::tf32_rna(x);
+    const size_t o = ((size_t)b * n + a) * ldF + c;
+    fhi[o] = hi;
+    flo[o] = tc::tf32_rna(x - hi);
+}
+
+// Cell gradients of a real window -> the window gradient as a TF32 pair (the
+// tensor-core path's spectrum carries no sign folding); grid (K, B)
+__global__ void quadT_real_tc_kernel(Geo g, const float* __restrict__ cgrad4, const float* __restrict__ wr,
+                                     float* __restrict__ ghi, float* __restrict__ glo, int ldW) {
+    const long long ncell = (long long)g.K * g.W;
+    const int k = blockIdx.x, b = blockIdx.y;
+    const float* cg = cgrad4 + (size_t)b * ncell * 4;
+    for (int q = threadIdx.x; q < g.W; q += blockDim.x) {
+        float ga = 0.f;
+        auto take = [&](int kc, int qc, int c) {
+            if (kc < 0 || qc < 0 || kc >= g.K || qc >= g.W) return;
+            ga += cg[((long long)kc * g.W + qc) * 4 + c];
+        };
+        take(k, q, 0);
+        take(k, q - 1, 1);
+        take(k - 1, q - 1, 2);
+        take(k - 1, q, 3);
+        const float y = wr[(size_t)b * ncell + (size_t)k * g.W + q];
+        ga *= 2.f;  // the vis pass records halves of dchi2/dA
+        const float gy = y < 0.f ? -ga : (y > 0.f ? ga : 0.f);
+        const float hi = tc::tf32_rna(gy);
+        const size_t o = ((size_t)b * g.K + k) * ldW + q;
+        ghi[o] = hi;
+        glo[o] = tc::tf32_rna(gy - hi);
+    }
+}
+
+// Adjoint of the sweep from dchi2/dF: the profile samples (linear
+// interpolation weights, binned in shared memory, one flush per CTA), the
+// inclination (dr/dinc = xs^2 tan(inc) / r) and the central pixel.  A CTA
+// takes kRowsPerCta folded rows of one model; grid (ceil((rmax+1)/kRowsPerCta), B).
+__global__ void sweep_adjoint_kernel(Geo g, const float* __restrict__ intensity, const ModelConst* __restrict__ mc,
+                                     const float* __restrict__ gF, int ldF, float* __restrict__ gI,
+                                     double* __restrict__ ginc, float* __restrict__ gcentral) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* gIs = reinterpret_cast<float*>(smem_raw);  // nr bins
+    __shared__ double sinc;
+    __shared__ int lo_bin, hi_bin;
+    const int b = blockIdx.y;
+    const ModelConst m = mc[b];
+    const float* Ib = intensity + (size_t)b * g.nr;
+    const int n = g.rmax + 1;
+    for (int i = threadIdx.x; i < g.nr; i += blockDim.x) gIs[i] = 0.f;
+    if (threadIdx.x == 0) {
+        lo_bin = g.nr;
+        hi_bin = -1;
+        sinc = 0.0;
+    }
+    __syncthreads();
+    float ginc_acc = 0.f;
+    int my_lo = g.nr, my_hi = -1;
+    const int a0 = blockIdx.x * kRowsPerCta;
+    const int a1 = min(n, a0 + kRowsPerCta);
+    for (int e = threadIdx.x; e < (a1 - a0) * n; e += blockDim.x) {
+        const int a = a0 + e / n, c = e % n;
+        const float xb = gF[((size_t)b * n + a) * ldF + c];
+        if (a == 0 && c == 0) {
+            gcentral[b] = xb;
+            continue;
+        }
+        const float y = i2f_small(a) * g.dxy;
+        const float x = i2f_small(c) * g.dxy;
+        const float xs = x * m.inv_cos_inc;
+        const float r = sqrtf(xs * xs + y * y);  // bit-identical to the forward sweep's radius
+        const float tR = (r - g.Rmin) * g.inv_dR;
+        if (!(tR < (float)(g.nr - 1))) continue;
+        int iR = 0;
+        if (tR > 0.f) {
+            float fl;
+            iR = floor_i(tR, &fl);
+        }
+        const float frac = (r - i2f_small(iR) * g.dR - g.Rmin) * g.inv_dR;
+        const float gxs = xb * g.sr_to_px;
+        const float I0 = __ldg(&Ib[iR]), I1 = __ldg(&Ib[iR + 1]);
+        atomicAdd(&gIs[iR], gxs * (1.f - frac));
+        atomicAdd(&gIs[iR + 1], gxs * frac);
+        my_lo = min(my_lo, iR);
+        my_hi = max(my_hi, iR + 1);
+        const float rinv = r > 0.f ? __fdividef(1.f, r) : 0.f;
+        ginc_acc += gxs * ((I1 - I0) * g.inv_dR) * (xs * xs * m.tan_inc) * rinv;
+    }
+    atomicMin(&lo_bin, my_lo);
+    atomicMax(&hi_bin, my_hi);
+    atomicAdd(&sinc, (double)ginc_acc);
+    __syncthreads();
+    float* gIb = gI + (size_t)b * g.nr;
+    for (int i = lo_bin + threadIdx.x; i <= hi_bin; i += blockDim.x)
+        if (gIs[i] != 0.f) atomicAdd(&gIb[i], gIs[i]);
+    if (threadIdx.x == 0) atomicAdd(&ginc[b], sinc);
+}
+
 // adjoint of the central pixel: I_bar += coef * x_bar(center)
 __global__ void central_adjoint_kernel(int B, int nr, const double* __restrict__ coef, int ncoef,
                                        const float* __restrict__ gcentral, float* __restrict__ gI) {
@@ -1269,7 +1409,7 @@ __global__ void __launch_bounds__(MAXT) rowsT_image_batch_kernel(Geo g, int F, c
 // ---------------------------------------------------------------------------
 using Shape = tune::Shape;
 struct TuneKey {
-    int N, K, W, R, B, nd, grad, nr, image;
+    int N, K, W, R, B, nd, grad, nr, image, tc;
     bool operator<(const TuneKey& o) const {
         return std::memcmp(this, &o, sizeof(TuneKey)) < 0;
     }
@@ -1397,9 +1537,85 @@ struct GraphEntry {
 };
 constexpr size_t kMaxGraphs = 32;
 
+// cosine matrices of the tensor-core spectrum passes (one geometry) as TF32
+// pairs in device memory; row-major with the leading dimensions below
+struct CosMats {
+    int ldF = 0, ldW = 0, ldK = 0;
+    float *ck_hi = nullptr, *ck_lo = nullptr;    // Ck   [K][ldF]
+    float *cv_hi = nullptr, *cv_lo = nullptr;    // Cv   [W][ldF]
+    float *cvt_hi = nullptr, *cvt_lo = nullptr;  // Cv^T [rmax+1][ldW]
+    float *ckt_hi = nullptr, *ckt_lo = nullptr;  // Ck^T [rmax+1][ldK]
+};
+inline int round4(int x) { return (x + 3) / 4 * 4; }
+// round to the nearest TF32 value, ties away from zero (cvt.rna.tf32.f32 on the host)
+inline float tf32_rna_host(float x) {
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    b += 0x1000u;
+    b &= ~0x1FFFu;
+    float r;
+    std::memcpy(&r, &b, 4);
+    return r;
+}
+
 struct BatchWs {
     std::mutex mu;
     Buf mc, coef, zt, win, partials, gsum, cgrad, gwin, zbar, ginc, gcentral, gI_tmp, state;
+    Buf tcF, tcD1, tcG, tcG1, tcGF;  // tensor-core passes: F, D1, window gradient, G1 (TF32 pairs), dchi2/dF
+    std::map<std::tuple<int, int, int, int, int>, CosMats> cos;
+    // Ck, Cv and their transposes for geometry g, built on the host in long double
+    const CosMats& cos_mats(int N, int K, int r0, int W, int rmax) {
+        const auto key = std::make_tuple(N, K, r0, W, rmax);
+        auto it = cos.find(key);
+        if (it != cos.end()) return it->second;
+        const int n = rmax + 1;
+        CosMats m;
+        m.ldF = round4(n);
+        m.ldW = round4(W);
+        m.ldK = round4(K);
+        const long double two_pi = 6.283185307179586476925286766559005768L;
+        auto wgt = [&](int j) { return (j == 0 || 2 * j == N) ? 1.0L : 2.0L; };
+        auto cosn = [&](long long p) { return cosl(two_pi * (long double)(p % N) / (long double)N); };
+        std::vector<float> ckh((size_t)K * m.ldF, 0.f), ckl(ckh.size(), 0.f);
+        std::vector<float> cvh((size_t)W * m.ldF, 0.f), cvl(cvh.size(), 0.f);
+        std::vector<float> cvth((size_t)n * m.ldW, 0.f), cvtl(cvth.size(), 0.f);
+        std::vector<float> ckth((size_t)n * m.ldK, 0.f), cktl(ckth.size(), 0.f);
+        auto put = [](std::vector<float>& h, std::vector<float>& l, size_t i, long double x) {
+            const float f = (float)x;
+            h[i] = tf32_rna_host(f);
+            l[i] = tf32_rna_host((float)(x - (long double)h[i]));
+        };
+        for (int k = 0; k < K; ++k)
+            for (int c = 0; c < n; ++c) {
+                const long double x = wgt(c) * cosn((long long)c * k);
+                put(ckh, ckl, (size_t)k * m.ldF + c, x);
+                put(ckth, cktl, (size_t)c * m.ldK + k, x);
+            }
+        for (int q = 0; q < W; ++q) {
+            const int rr = std::abs(r0 + q - N / 2);
+            for (int a = 0; a < n; ++a) {
+                const long double x = wgt(a) * cosn((long long)a * rr);
+                put(cvh, cvl, (size_t)q * m.ldF + a, x);
+                put(cvth, cvtl, (size_t)a * m.ldW + q, x);
+            }
+        }
+        auto up = [](const std::vector<float>& h) {
+            float* d = nullptr;
+            cudaError_t e = cudaMalloc(&d, sizeof(float) * h.size());
+            if (e == cudaSuccess) e = cudaMemcpy(d, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) throw e;
+            return d;
+        };
+        m.ck_hi = up(ckh);
+        m.ck_lo = up(ckl);
+        m.cv_hi = up(cvh);
+        m.cv_lo = up(cvl);
+        m.cvt_hi = up(cvth);
+        m.cvt_lo = up(cvtl);
+        m.ckt_hi = up(ckth);
+        m.ckt_lo = up(cktl);
+        return cos.emplace(key, m).first->second;
+    }
     Buf in_I, in_p, out_chi2, out_sets, out_gI, out_gp;  // staging of graph launches
     std::map<GraphKey, GraphEntry> graphs;
     cudaStream_t cap = nullptr;  // capture stream (captures cannot use the legacy default stream)
@@ -1505,6 +1721,40 @@ template <class F> int bguard(F&& f) {
         set_error_message(e.what());
         return GALARIO_ERUNTIME;
     }
+}
+
+// the tensor-core spectrum passes: GALARIO_TC=0 keeps the FFT passes
+bool tc_enabled() {
+    const char* v = std::getenv("GALARIO_TC");
+    return !(v && v[0] == '0');
+}
+
+// One batched product C[z] = A[z] B[z]^T on the tensor cores (gb_tc.cuh), the
+// N tile chosen to waste the fewest columns (ties: the wider tile).
+template <int BN>
+void tc_launch_bn(const tc::Operand& A, const tc::Operand& Bo, const tc::Params& p, int batch, cudaStream_t s) {
+    CUtensorMap ah, al, bh, bl;
+    if (!tc::make_map(&ah, A.hi, A, tc::BM) || !tc::make_map(&al, A.lo, A, tc::BM) ||
+        !tc::make_map(&bh, Bo.hi, Bo, BN) || !tc::make_map(&bl, Bo.lo, Bo, BN))
+        throw Err{GALARIO_ERUNTIME, "Error in batch: cannot encode a tensor map"};
+    BCK((cudaError_t)smem_attr((const void*)tc::gemm_3xtf32_kernel<BN>, tc::Cfg<BN>::kSmem));
+    const dim3 grid((p.M + tc::BM - 1) / tc::BM, (p.N + BN - 1) / BN, batch);
+    tc::gemm_3xtf32_kernel<BN><<<grid, tc::kThreads, tc::Cfg<BN>::kSmem, s>>>(ah, al, bh, bl, p);
+    BCK(cudaGetLastError());
+}
+void tc_gemm(const tc::Operand& A, const tc::Operand& Bo, const tc::Params& p, int batch, cudaStream_t s) {
+    const int cand[2] = {128, 64};
+    int best = 128;
+    long long waste = 1LL << 60;
+    for (int bn : cand) {
+        const long long w = (long long)((p.N + bn - 1) / bn) * bn - p.N;
+        if (w < waste) {
+            waste = w;
+            best = bn;
+        }
+    }
+    if (best == 128) tc_launch_bn<128>(A, Bo, p, batch, s);
+    else tc_launch_bn<64>(A, Bo, p, batch, s);
 }
 
 __global__ void extent_f32_kernel(const float* __restrict__ u, const float* __restrict__ v, int nd,
@@ -1908,6 +2158,24 @@ static void batch_run(const BatchCall& call) {
         if (Bg > B) Bg = B;
         const int ngroups = (B + Bg - 1) / Bg;
 
+        // tensor-core spectrum passes for swept profiles (products with the
+        // cosine matrices) where the folded quadrant, the window and the
+        // profile bins fit; the FFT passes otherwise
+        const int nF = g.rmax + 1;
+        const bool use_tc = real && tc_enabled() && tc::encode_fn() != nullptr && nF <= 2048 && g.K <= 2048 &&
+                            g.W <= 4096 && (size_t)nr * sizeof(float) <= 160 * 1024;
+        const CosMats* cm = use_tc ? &ws.cos_mats(g.N, g.K, g.r0, g.W, g.rmax) : nullptr;
+        float *tF = nullptr, *tD1 = nullptr, *tG = nullptr, *tG1 = nullptr, *tGF = nullptr;
+        if (use_tc) {
+            tF = ws.tcF.get<float>((size_t)2 * B * nF * cm->ldF);
+            tD1 = ws.tcD1.get<float>((size_t)2 * B * g.K * cm->ldF);
+            if (grad) {
+                tG = ws.tcG.get<float>((size_t)2 * B * g.K * cm->ldW);
+                tG1 = ws.tcG1.get<float>((size_t)2 * B * nF * cm->ldK);
+                tGF = ws.tcGF.get<float>((size_t)B * nF * cm->ldF);
+            }
+        }
+
         // folded rows per staging group of the row passes: 2F rows x K columns
         // within 20 KiB; the adjoint runs G groups per CTA to amortise its flush
         const int Fcap = std::max(1, (int)((20 * 1024) / (sizeof(float2) * 2 * (size_t)g.K) - 1));
@@ -2058,6 +2326,43 @@ static void batch_run(const BatchCall& call) {
             });
             BCK(cudaGetLastError());
         };
+        // forward spectrum passes on the tensor cores: F -> D1 = Ck F^T -> S = D1 Cv^T
+        auto tc_forward = [&] {
+            const size_t sF = (size_t)nF * cm->ldF, sD = (size_t)g.K * cm->ldF;
+            sweep_fold_kernel<<<dim3((nF * nF + 255) / 256, B), 256, 0, s>>>(g, intensity, mc, tF, tF + B * sF,
+                                                                             cm->ldF);
+            BCK(cudaGetLastError());
+            const tc::Operand a1{cm->ck_hi, cm->ck_lo, g.K, nF, cm->ldF, 0, 1};
+            const tc::Operand b1{tF, tF + B * sF, nF, nF, cm->ldF, (long long)sF, B};
+            const tc::Params p1{g.K, nF, nF, tD1, tD1 + B * sD, (long long)sD, cm->ldF, tc::kStoreTf32, 0, 1, &st->err};
+            tc_gemm(a1, b1, p1, B, s);
+            const tc::Operand a2{tD1, tD1 + B * sD, g.K, nF, cm->ldF, (long long)sD, B};
+            const tc::Operand b2{cm->cv_hi, cm->cv_lo, g.W, nF, cm->ldF, 0, 1};
+            const tc::Params p2{g.K, g.W, nF, reinterpret_cast<float*>(wel), nullptr, (long long)ncell, g.W,
+                                tc::kStore, 1, 0, &st->err};
+            tc_gemm(a2, b2, p2, B, s);
+        };
+        // adjoint on the tensor cores: window gradient G -> G1 = Cv^T G^T -> dchi2/dF = G1 Ck -> sweep adjoint
+        auto tc_adjoint = [&] {
+            const size_t sG = (size_t)g.K * cm->ldW, sG1 = (size_t)nF * cm->ldK, sF = (size_t)nF * cm->ldF;
+            quadT_real_tc_kernel<<<dim3(g.K, B), 256, 0, s>>>(g, cgrad, reinterpret_cast<const float*>(wel), tG,
+                                                              tG + B * sG, cm->ldW);
+            BCK(cudaGetLastError());
+            const tc::Operand a1{cm->cvt_hi, cm->cvt_lo, nF, g.W, cm->ldW, 0, 1};
+            const tc::Operand b1{tG, tG + B * sG, g.K, g.W, cm->ldW, (long long)sG, B};
+            const tc::Params p1{nF, g.K, g.W, tG1, tG1 + B * sG1, (long long)sG1, cm->ldK, tc::kStoreTf32, 0, 1,
+                                &st->err};
+            tc_gemm(a1, b1, p1, B, s);
+            const tc::Operand a2{tG1, tG1 + B * sG1, nF, g.K, cm->ldK, (long long)sG1, B};
+            const tc::Operand b2{cm->ckt_hi, cm->ckt_lo, nF, g.K, cm->ldK, 0, 1};
+            const tc::Params p2{nF, nF, g.K, tGF, nullptr, (long long)sF, cm->ldF, tc::kStore, 1, 0, &st->err};
+            tc_gemm(a2, b2, p2, B, s);
+            const size_t smA = sizeof(float) * nr;
+            BCK((cudaError_t)smem_attr((const void*)sweep_adjoint_kernel, smA));
+            sweep_adjoint_kernel<<<dim3((nF + kRowsPerCta - 1) / kRowsPerCta, B), 256, smA, s>>>(
+                g, intensity, mc, tGF, cm->ldF, grad_intensity, ginc_d, gcentral);
+            BCK(cudaGetLastError());
+        };
         auto zero_grads = [&] {
             BCK(cudaMemsetAsync(cgrad, 0, sizeof(float) * (size_t)B * ncell * recf, s));
             BCK(cudaMemsetAsync(ginc_d, 0, sizeof(double) * B, s));
@@ -2072,8 +2377,12 @@ static void batch_run(const BatchCall& call) {
             model_setup_kernel<<<(B + 31) / 32, 32, 0, s>>>(B, params, pstride, intensity, nr, coef_d, ncoef, inv_duv,
                                                              mc);
             BCK(cudaGetLastError());
-            rows(sh.e_rows);
-            cols(sh.e_cols);
+            if (use_tc) {
+                tc_forward();
+            } else {
+                rows(sh.e_rows);
+                cols(sh.e_cols);
+            }
             if (grad) zero_grads();
             vis(sh.pts);
             batch_finalize_kernel<<<dim3(B, grad ? kAcc : 1), 256, 0, s>>>(
@@ -2081,14 +2390,18 @@ static void batch_run(const BatchCall& call) {
             BCK(cudaGetLastError());
             if (!grad) return;
             // ---- adjoint ----
-            if (real)
-                quadT_real_kernel<<<dim3(g.K, B), 256, 0, s>>>(g, cgrad, reinterpret_cast<const float*>(wel),
-                                                               reinterpret_cast<float*>(gwin));
-            else
-                quadT_batch_kernel<<<dim3(g.K, B), 256, 0, s>>>(g, cgrad, wel, gwin);
-            BCK(cudaGetLastError());
-            colsT(sh.e_colsT);
-            rowsT(sh.e_rowsT);
+            if (use_tc) {
+                tc_adjoint();
+            } else {
+                if (real)
+                    quadT_real_kernel<<<dim3(g.K, B), 256, 0, s>>>(g, cgrad, reinterpret_cast<const float*>(wel),
+                                                                   reinterpret_cast<float*>(gwin));
+                else
+                    quadT_batch_kernel<<<dim3(g.K, B), 256, 0, s>>>(g, cgrad, wel, gwin);
+                BCK(cudaGetLastError());
+                colsT(sh.e_colsT);
+                rowsT(sh.e_rowsT);
+            }
             if (!image) {
                 central_adjoint_kernel<<<B, 64, 0, s>>>(B, nr, coef_d, ncoef, gcentral, grad_intensity);
                 BCK(cudaGetLastError());
@@ -2101,13 +2414,14 @@ static void batch_run(const BatchCall& call) {
         // Coordinate descent over the passes, every candidate timed inside a
         // complete call (so that each pass sees the cache state it has in
         // production), best of three interleaved timings.
-        const TuneKey key{g.N, g.K, g.W, g.R, B, d->nd_pad, grad ? 1 : 0, nr, image ? 1 : 0};
+        const TuneKey key{g.N, g.K, g.W, g.R, B, d->nd_pad, grad ? 1 : 0, nr, image ? 1 : 0, use_tc ? 1 : 0};
         auto it = ws.shapes.find(key);
         const bool tuned = it != ws.shapes.end();
         tune::Key fkey;
         Shape fsh;
         const bool from_file = !tuned && autotune_enabled() &&
-                               (fkey = tune_file_key(g.N, g.K, g.W, g.R, B, d->nd_pad, grad ? 1 : 0, nr, image ? 1 : 0),
+                               (fkey = tune_file_key(g.N, g.K, g.W, g.R, B, d->nd_pad, grad ? 1 : 0, nr,
+                                                      image ? 1 : (use_tc ? 2 : 0)),
                                 tune_file().lookup(fkey, &fsh)) &&
                                shape_valid(g, fsh, real, tma_ok);
         if (tuned) {
@@ -2120,15 +2434,18 @@ static void batch_run(const BatchCall& call) {
             std::vector<int> col_shapes = fft_candidates(g.N);
             if (tma_ok)
                 for (int e : fft_candidates(g.N)) col_shapes.push_back(e + kTmaCols);
-            sh.e_rows = tu.best(fft_candidates(g.M), [&](int e) { sh.e_rows = e; run_all(); });
-            sh.e_cols = tu.best(col_shapes, [&](int e) { sh.e_cols = e; run_all(); });
+            // the tensor-core passes have no FFT shapes to tune
+            if (!use_tc) {
+                sh.e_rows = tu.best(fft_candidates(g.M), [&](int e) { sh.e_rows = e; run_all(); });
+                sh.e_cols = tu.best(col_shapes, [&](int e) { sh.e_cols = e; run_all(); });
+            }
             // the visibility pass alone decides its shape (the spectrum passes
             // before it do not depend on it and only add noise): one complete
             // call sets up the window, then each candidate reruns the pass
             // (the gradient records it accumulates are zeroed by the next call)
             run_all();
             sh.pts = tu.best(real ? std::vector<int>{2, 4, 8} : std::vector<int>{2, 4}, [&](int p) { vis(p); });
-            if (grad) {
+            if (grad && !use_tc) {
                 sh.e_colsT = tu.best(fft_candidates(g.N), [&](int e) { sh.e_colsT = e; run_all(); });
                 sh.e_rowsT = tu.best(fft_candidates(g.M), [&](int e) { sh.e_rowsT = e; run_all(); });
             }

@@ -7,7 +7,9 @@
 //
 //   <gpu> f32 <N> <K> <W> <R> <B> <nvis bucket> <grad> <nr> <image> : <e_rows> <e_cols> <e_colsT> <e_rowsT> <pts>
 //
-// <gpu> is the device name with blanks replaced by '_'; the visibility count
+// <gpu> is the device name with blanks replaced by '_'; <image> is the pass
+// variant (0 profiles with FFT passes, 1 images, 2 profiles with tensor-core
+// passes); the visibility count
 // enters as its bucket, ceil(log2(padded visibilities)), so datasets of
 // similar size share an entry.  Lines that do not parse are skipped; when a
 // key appears more than once the last line wins.  Path: GALARIO_TUNE_CACHE if
