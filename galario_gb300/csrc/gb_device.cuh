@@ -583,6 +583,26 @@ __device__ __forceinline__ DF df_add(DF a, DF b) {
     DF s = df_two_sum(a.hi, b.hi);
     return df_renorm(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
+// Block sum of FP32 values: double-float warp sums (FP32 instructions only;
+// GB300's FP64 pipe runs at a 64th of the FP32 rate), the warp totals added in
+// FP64 by thread 0.  Valid in thread 0.
+__device__ __forceinline__ double block_sum_df(float x, double* sh) {
+    DF s{x, 0.f};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h = __shfl_xor_sync(0xffffffffu, s.hi, o);
+        const float l = __shfl_xor_sync(0xffffffffu, s.lo, o);
+        s = df_add(s, DF{h, l});
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = (double)s.hi + (double)s.lo;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < nw; ++q) t += sh[q];
+    return t;  // valid in thread 0
+}
 // floor of x = hi + lo (|hi| < 2^22, |lo| at most a few ulps of hi) as an
 // integer and the fraction in [0, 1]: n = rint(hi) by the magic-number
 // method, hi - n is exact (Sterbenz), f = (hi - n) + lo lies in

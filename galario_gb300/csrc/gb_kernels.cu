@@ -22,11 +22,14 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <type_traits>
 
 #include "gb_device.cuh"
 #include "gb_internal.cuh"
+#include "gb_tc.cuh"
 
 namespace gbg {
 
@@ -58,6 +61,63 @@ __global__ void __launch_bounds__(MAXT) rows_image_kernel(const T* __restrict__ 
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
         CT x = real_split<T>(buf, M, k, tw);
         zt[(size_t)k * N + i] = CT{sgn * x.x, sgn * x.y};
+    }
+}
+
+// FP32 image rows with the loads pipelined: persistent CTAs take the rows
+// i = blockIdx.x, blockIdx.x + gridDim.x, ...; the next row is fetched by a 1D
+// bulk copy (cp.async.bulk, completion counted on an mbarrier) into the other
+// of two staging buffers while the current row is transformed, so HBM reads
+// overlap the shared-memory FFT.  Needs N * 4 bytes a multiple of 16 and a
+// 16-byte aligned image.  Waits are bounded: one that gives up sets ERR_SPIN,
+// waits (bounded) for the copy it has in flight and ends the CTA.
+template <int E, int MAXT>
+__global__ void __launch_bounds__(MAXT) rows_image_tma_kernel(const float* __restrict__ image, int N,
+                                                              const float2* __restrict__ tw,
+                                                              const float2* __restrict__ stw,
+                                                              float2* __restrict__ zt, int host_K, DevState* st,
+                                                              int row_sign) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int M = N / 2;
+    float* stg = reinterpret_cast<float*>(smem_raw);                  // [2][N]
+    float2* buf = reinterpret_cast<float2*>(stg + 2 * (size_t)N);     // fft_slots(M)
+    uint64_t* bar = reinterpret_cast<uint64_t*>(buf + fft_slots(M));  // [2]
+    const uint32_t bytes = (uint32_t)N * 4u;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int K = get_window(host_K, 0, 0, st).K;
+    int i = blockIdx.x;
+    if (threadIdx.x == 0 && i < N) tc::bulk_load_1d(stg, image + (size_t)i * N, bytes, &bar[0]);
+    for (int it = 0; i < N; ++it, i += gridDim.x) {
+        const int cur = it & 1;
+        const int nxt = i + gridDim.x;
+        if (threadIdx.x == 0 && nxt < N) {
+            // the other buffer was read through the generic proxy before the last barrier
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            tc::bulk_load_1d(stg + (size_t)(cur ^ 1) * N, image + (size_t)nxt * N, bytes, &bar[cur ^ 1]);
+        }
+        const bool ok = tc::mbar_wait(&bar[cur], (uint32_t)((it >> 1) & 1));
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0) {
+                atomicOr(&st->err, ERR_SPIN);
+                if (nxt < N) (void)tc::mbar_wait(&bar[cur ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
+            }
+            return;
+        }
+        const float2* row = reinterpret_cast<const float2*>(stg + (size_t)cur * N);
+        for (int m = threadIdx.x; m < M; m += blockDim.x) buf[sp(m)] = row[m];
+        __syncthreads();
+        block_fft<float, E>(buf, M, ilog2(M), stw);
+        const float sgn = (row_sign && (i & 1)) ? -1.f : 1.f;
+        for (int k = threadIdx.x; k < K; k += blockDim.x) {
+            const float2 x = real_split<float>(buf, M, k, tw);
+            zt[(size_t)k * N + i] = make_float2(sgn * x.x, sgn * x.y);
+        }
+        __syncthreads();  // buf and this staging buffer are free again
     }
 }
 
@@ -882,7 +942,9 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 8 && REALQ) ? 4 : 1) vis_ke
         atomicCAS(&a.state->err_index, 0ull, (unsigned long long)(err_idx + 1));
     }
     if (CHI2) {
-        const double tot = block_sum((double)acc, sh);
+        double tot;
+        if constexpr (sizeof(T) == 4) tot = block_sum_df(acc, sh);
+        else tot = block_sum((double)acc, sh);
         grid_finish(tot, a.partials, a.state, a.chi2_out, a.part_off, a.parts_total);
     }
 }
@@ -1053,6 +1115,12 @@ int num_sms() {
 // ===========================================================================
 template <typename T> int Launch<T>::max_fft_n() { return max_fft_n_impl<T>(); }
 
+// GALARIO_ROWS_TMA=0 keeps the one-row-per-CTA image row pass
+bool rows_tma_enabled() {
+    const char* v = std::getenv("GALARIO_ROWS_TMA");
+    return !(v && v[0] == '0');
+}
+
 template <typename T>
 cudaError_t Launch<T>::extent(const T* u, const T* v, int nd, int N, double duv, DevState* state, cudaStream_t s) {
     int blocks = (nd + 255) / 256;
@@ -1095,6 +1163,27 @@ cudaError_t Launch<T>::rows_image(const T* image, int N, const CT* tw, const CT*
         const int M = N / 2;
         FftCfg<T> c = fft_cfg<T>(M);
         cudaError_t e = cudaSuccess;
+        // FP32: the pipelined variant where its staging fits (N * 4 bytes a
+        // multiple of 16, a 16-byte aligned image)
+        const size_t sm_tma = 2 * sizeof(float) * (size_t)N + c.smem + 2 * sizeof(uint64_t);
+        if constexpr (sizeof(T) == 4) {
+            if (N >= 64 && (N % 4) == 0 && ((reinterpret_cast<uintptr_t>(image) & 15) == 0) &&
+                sm_tma <= 200 * 1024 && rows_tma_enabled()) {
+                GBG_DISPATCH_E(c.E, c.threads, {
+                    auto kern = rows_image_tma_kernel<EE, TT>;
+                    e = set_smem(kern, sm_tma);
+                    int per_sm = 0;
+                    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, c.threads, sm_tma);
+                    if (e == cudaSuccess) {
+                        const int grid = std::max(1, std::min(N, num_sms() * std::max(per_sm, 1)));
+                        kern<<<grid, c.threads, sm_tma, s>>>(image, N, tw, stw, zt, host_K,
+                                                             const_cast<DevState*>(state), row_sign ? 1 : 0);
+                        e = cudaGetLastError();
+                    }
+                });
+                return e;
+            }
+        }
         GBG_DISPATCH_E(c.E, c.threads, {
             auto kern = rows_image_kernel<T, EE, TT>;
             e = set_smem(kern, c.smem);
