@@ -140,8 +140,12 @@ def test_config4_parameter_gradient_vs_torch_fp64(sets, walkers64):
 
 
 def test_config4_parameter_gradient_vs_fd_oracle(sets, walkers64, oracle_port):
-    """FP64 central finite differences (h = 1e-6 relative) of the oracle's
-    chi2Profile over all 8 sets, for two walkers."""
+    """FP64 central finite differences of the oracle's chi2Profile over all 8
+    sets, for two walkers.  The step is 1e-9 relative: chi2 of the reference
+    jumps where a visibility's interpolated real spectrum changes sign
+    (V = A sign(z)), and a step of 1e-6 relative already crosses such a jump
+    on 7.7M visibilities (it moved d chi2/d r0 by 7 % for walker 3); the FP64
+    evaluation noise at 1e-9 is about 1e-6 of the gradient."""
     import torch
     from grad_conditioning import gpu_gradient, reference_gradient, ring_profile_t
     c = sets
@@ -163,13 +167,14 @@ def test_config4_parameter_gradient_vs_fd_oracle(sets, walkers64, oracle_port):
         _, _, kappa, _, _, amb_g = reference_gradient(thetas[i].cuda(), geo, t["u"], t["v"], t["re"], t["im"],
                                                        t["w"])
         base = walkers64[b]
+        scale = (1.0, 1.0, 1.0, 1.0, 1.0, arcsec, arcsec)  # floors of the step: 1e-9 of these
         for j in range(7):
-            h = 1e-6 * abs(base[j])
+            h = 1e-9 * max(abs(base[j]), scale[j])
             pp, pm = base.copy(), base.copy()
             pp[j] += h
             pm[j] -= h
             fd = (chi2_at(pp) - chi2_at(pm)) / (2 * h)
-            assert abs(grad[i, j] - fd) <= (KAPPA_C * U32 * kappa[j] + 1e-6) * abs(fd) + amb_g[j], \
+            assert abs(grad[i, j] - fd) <= (KAPPA_C * U32 * kappa[j] + 1e-5) * abs(fd) + amb_g[j], \
                 (b, j, grad[i, j], fd)
 
 
