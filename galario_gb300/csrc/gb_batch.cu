@@ -601,8 +601,9 @@ __device__ __forceinline__ float real_point(const Geo& g, const ModelConst& m, c
     const float A = fmaf(q, dAq, fmaf(t, a1 - a0, a0));
     const float z = fmaf(q, fmaf(t, (y0 - y1) + (y2 - y3), y3 - y0), fmaf(t, y1 - y0, y0));
     const float As = z < 0.f ? -A : A;
-    float ps, pc;
-    sincos2pi_df(df_dot2(u, m.dra, v, m.ddec), &ps, &pc);
+    float ps = 0.f, pc = 1.f;
+    // the model is the same for the whole warp: no divergence
+    if (m.phase) sincos2pi_df(df_dot2(u, m.dra, v, m.ddec), &ps, &pc);
     const float vx = As * pc, vy = As * ps;
     const float dr = vx - re, di = vy - im;
     const float hx = w * dr, hy = w * di;  // (dchi2/dV) / 2
@@ -1215,29 +1216,25 @@ __global__ void quadT_real_tc_kernel(Geo g, const float* __restrict__ cgrad4, co
 }
 
 // Adjoint of the sweep from dchi2/dF: the profile samples (linear
-// interpolation weights, binned in shared memory, one flush per CTA), the
-// inclination (dr/dinc = xs^2 tan(inc) / r) and the central pixel.  A CTA
-// takes kRowsPerCta folded rows of one model; grid (ceil((rmax+1)/kRowsPerCta), B).
+// interpolation weights, binned in shared memory), the inclination
+// (dr/dinc = xs^2 tan(inc) / r) and the central pixel.  A CTA takes
+// kRowsPerCta folded rows of one model and writes its nr bins and its
+// inclination sum as one partial (no global atomics);
+// sweep_adjoint_reduce_kernel adds the partials in a fixed order.
+// Grid (nchunk = ceil((rmax+1)/kRowsPerCta), B).
 __global__ void sweep_adjoint_kernel(Geo g, const float* __restrict__ intensity, const ModelConst* __restrict__ mc,
-                                     const float* __restrict__ gF, int ldF, float* __restrict__ gI,
-                                     double* __restrict__ ginc, float* __restrict__ gcentral) {
+                                     const float* __restrict__ gF, int ldF, float* __restrict__ part,
+                                     double* __restrict__ part_inc, float* __restrict__ gcentral) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* gIs = reinterpret_cast<float*>(smem_raw);  // nr bins
-    __shared__ double sinc;
-    __shared__ int lo_bin, hi_bin;
+    __shared__ double sh[32];
     const int b = blockIdx.y;
     const ModelConst m = mc[b];
     const float* Ib = intensity + (size_t)b * g.nr;
     const int n = g.rmax + 1;
     for (int i = threadIdx.x; i < g.nr; i += blockDim.x) gIs[i] = 0.f;
-    if (threadIdx.x == 0) {
-        lo_bin = g.nr;
-        hi_bin = -1;
-        sinc = 0.0;
-    }
     __syncthreads();
     float ginc_acc = 0.f;
-    int my_lo = g.nr, my_hi = -1;
     const int a0 = blockIdx.x * kRowsPerCta;
     const int a1 = min(n, a0 + kRowsPerCta);
     for (int e = threadIdx.x; e < (a1 - a0) * n; e += blockDim.x) {
@@ -1263,19 +1260,34 @@ __global__ void sweep_adjoint_kernel(Geo g, const float* __restrict__ intensity,
         const float I0 = __ldg(&Ib[iR]), I1 = __ldg(&Ib[iR + 1]);
         atomicAdd(&gIs[iR], gxs * (1.f - frac));
         atomicAdd(&gIs[iR + 1], gxs * frac);
-        my_lo = min(my_lo, iR);
-        my_hi = max(my_hi, iR + 1);
         const float rinv = r > 0.f ? __fdividef(1.f, r) : 0.f;
         ginc_acc += gxs * ((I1 - I0) * g.inv_dR) * (xs * xs * m.tan_inc) * rinv;
     }
-    atomicMin(&lo_bin, my_lo);
-    atomicMax(&hi_bin, my_hi);
-    atomicAdd(&sinc, (double)ginc_acc);
+    const double tot = block_sum_df(ginc_acc, sh);  // FP32 instructions only
     __syncthreads();
-    float* gIb = gI + (size_t)b * g.nr;
-    for (int i = lo_bin + threadIdx.x; i <= hi_bin; i += blockDim.x)
-        if (gIs[i] != 0.f) atomicAdd(&gIb[i], gIs[i]);
-    if (threadIdx.x == 0) atomicAdd(&ginc[b], sinc);
+    float* pb = part + ((size_t)b * gridDim.x + blockIdx.x) * g.nr;
+    for (int i = threadIdx.x; i < g.nr; i += blockDim.x) pb[i] = gIs[i];
+    if (threadIdx.x == 0) part_inc[(size_t)b * gridDim.x + blockIdx.x] = tot;
+}
+
+// gI[b][i] = sum of the nchunk partial bins of model b (fixed order),
+// ginc[b] = sum of the partial inclination sums.  Grid (ceil(nr/256), B).
+__global__ void sweep_adjoint_reduce_kernel(int nr, int nchunk, const float* __restrict__ part,
+                                            const double* __restrict__ part_inc, float* __restrict__ gI,
+                                            double* __restrict__ ginc) {
+    const int b = blockIdx.y;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nr) {
+        const float* pb = part + (size_t)b * nchunk * nr + i;
+        float s = 0.f;
+        for (int q = 0; q < nchunk; ++q) s += pb[(size_t)q * nr];
+        gI[(size_t)b * nr + i] = s;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < nchunk; ++q) t += part_inc[(size_t)b * nchunk + q];
+        ginc[b] = t;
+    }
 }
 
 // adjoint of the central pixel: I_bar += coef * x_bar(center)
@@ -1562,6 +1574,7 @@ struct BatchWs {
     std::mutex mu;
     Buf mc, coef, zt, win, partials, gsum, cgrad, gwin, zbar, ginc, gcentral, gI_tmp, state;
     Buf tcF, tcD1, tcG, tcG1, tcGF;  // tensor-core passes: F, D1, window gradient, G1 (TF32 pairs), dchi2/dF
+    Buf tcPart, tcPinc;               // sweep adjoint: per-CTA partial profile bins and inclination sums
     std::map<std::tuple<int, int, int, int, int>, CosMats> cos;
     // Ck, Cv and their transposes for geometry g, built on the host in long double
     const CosMats& cos_mats(int N, int K, int r0, int W, int rmax) {
@@ -2165,7 +2178,8 @@ static void batch_run(const BatchCall& call) {
         const bool use_tc = real && tc_enabled() && tc::encode_fn() != nullptr && nF <= 2048 && g.K <= 2048 &&
                             g.W <= 4096 && (size_t)nr * sizeof(float) <= 160 * 1024;
         const CosMats* cm = use_tc ? &ws.cos_mats(g.N, g.K, g.r0, g.W, g.rmax) : nullptr;
-        float *tF = nullptr, *tD1 = nullptr, *tG = nullptr, *tG1 = nullptr, *tGF = nullptr;
+        float *tF = nullptr, *tD1 = nullptr, *tG = nullptr, *tG1 = nullptr, *tGF = nullptr, *tPart = nullptr;
+        double* tPinc = nullptr;
         if (use_tc) {
             tF = ws.tcF.get<float>((size_t)2 * B * nF * cm->ldF);
             tD1 = ws.tcD1.get<float>((size_t)2 * B * g.K * cm->ldF);
@@ -2173,6 +2187,9 @@ static void batch_run(const BatchCall& call) {
                 tG = ws.tcG.get<float>((size_t)2 * B * g.K * cm->ldW);
                 tG1 = ws.tcG1.get<float>((size_t)2 * B * nF * cm->ldK);
                 tGF = ws.tcGF.get<float>((size_t)B * nF * cm->ldF);
+                const size_t nchunk = (size_t)(nF + kRowsPerCta - 1) / kRowsPerCta;
+                tPart = ws.tcPart.get<float>((size_t)B * nchunk * nr);
+                tPinc = ws.tcPinc.get<double>((size_t)B * nchunk);
             }
         }
 
@@ -2358,9 +2375,13 @@ static void batch_run(const BatchCall& call) {
             const tc::Params p2{nF, nF, g.K, tGF, nullptr, (long long)sF, cm->ldF, tc::kStore, 1, 0, &st->err};
             tc_gemm(a2, b2, p2, B, s);
             const size_t smA = sizeof(float) * nr;
+            const int nchunk = (nF + kRowsPerCta - 1) / kRowsPerCta;
             BCK((cudaError_t)smem_attr((const void*)sweep_adjoint_kernel, smA));
-            sweep_adjoint_kernel<<<dim3((nF + kRowsPerCta - 1) / kRowsPerCta, B), 256, smA, s>>>(
-                g, intensity, mc, tGF, cm->ldF, grad_intensity, ginc_d, gcentral);
+            sweep_adjoint_kernel<<<dim3(nchunk, B), 256, smA, s>>>(g, intensity, mc, tGF, cm->ldF, tPart, tPinc,
+                                                                   gcentral);
+            BCK(cudaGetLastError());
+            sweep_adjoint_reduce_kernel<<<dim3((nr + 255) / 256, B), 256, 0, s>>>(nr, nchunk, tPart, tPinc,
+                                                                                 grad_intensity, ginc_d);
             BCK(cudaGetLastError());
         };
         auto zero_grads = [&] {

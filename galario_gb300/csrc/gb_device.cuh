@@ -399,6 +399,100 @@ __device__ __forceinline__ T sweep_pixel(int I, int J, const T* __restrict__ int
 
 
 // ---------------------------------------------------------------------------
+// Mixed-radix Stockham FFT (radices 2, 3, 4, 5, 7) for lengths that are not
+// powers of two: the same autosort scheme as block_fft (Govindaraju et al.,
+// SC 2008), one radix-R stage after the other with Ns = the product of the
+// previous radices: for j < L/R, k = j mod Ns, the R values
+// in[j + m L/R] times exp(-2 pi i m k / (Ns R)) go through an R-point DFT and
+// land at out[(j / Ns) Ns R + k + m Ns].  Stages alternate between two
+// shared-memory buffers.  Twiddles and the R-th roots of unity come from a
+// table built on the host in long double (MixPlan offsets).
+// ---------------------------------------------------------------------------
+constexpr int kMixMaxStages = 24;
+struct MixPlan {
+    int L, nst;
+    int R[kMixMaxStages], Ns[kMixMaxStages], off[kMixMaxStages];
+    int root_off[8];  // offset of exp(-2 pi i j / R), j < R, for R = 3, 5, 7
+};
+
+template <typename T, int R>
+__device__ __forceinline__ void mix_dft(C2<T>* x, const C2<T>* __restrict__ root) {
+    using CT = C2<T>;
+    if constexpr (R == 2) {
+        const CT a = x[0], b = x[1];
+        x[0] = cadd(a, b);
+        x[1] = CT{a.x - b.x, a.y - b.y};
+    } else if constexpr (R == 4) {
+        const CT t0 = cadd(x[0], x[2]), t1 = CT{x[0].x - x[2].x, x[0].y - x[2].y};
+        const CT t2 = cadd(x[1], x[3]), d = CT{x[1].x - x[3].x, x[1].y - x[3].y};
+        const CT t3 = CT{d.y, -d.x};  // -i (x1 - x3)
+        x[0] = cadd(t0, t2);
+        x[2] = CT{t0.x - t2.x, t0.y - t2.y};
+        x[1] = cadd(t1, t3);
+        x[3] = CT{t1.x - t3.x, t1.y - t3.y};
+    } else {
+        CT w[R];
+#pragma unroll
+        for (int j = 0; j < R; ++j) w[j] = __ldg(&root[j]);
+        CT y[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+            CT acc = x[0];
+#pragma unroll
+            for (int m = 1; m < R; ++m) acc = cadd(acc, cmul(x[m], w[(m * q) % R]));
+            y[q] = acc;
+        }
+#pragma unroll
+        for (int q = 0; q < R; ++q) x[q] = y[q];
+    }
+}
+
+template <typename T, int R>
+__device__ __forceinline__ void mix_stage(const C2<T>* in, C2<T>* out, int L, int Ns, const C2<T>* __restrict__ tw,
+                                          const C2<T>* __restrict__ root) {
+    using CT = C2<T>;
+    const int nb = L / R;
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+        const int k = j % Ns;
+        CT x[R];
+#pragma unroll
+        for (int m = 0; m < R; ++m) x[m] = in[j + m * nb];
+        if (Ns > 1) {
+#pragma unroll
+            for (int m = 1; m < R; ++m) x[m] = cmul(x[m], __ldg(&tw[(m - 1) * Ns + k]));
+        }
+        mix_dft<T, R>(x, root);
+        const int base = (j / Ns) * Ns * R + k;
+#pragma unroll
+        for (int m = 0; m < R; ++m) out[base + m * Ns] = x[m];
+    }
+}
+
+// the transform of the L values in a (b: scratch of L values); returns the
+// buffer that holds the result, in natural order
+template <typename T>
+__device__ C2<T>* block_fft_mixed(C2<T>* a, C2<T>* b, const MixPlan& p, const C2<T>* __restrict__ tab) {
+    C2<T>* in = a;
+    C2<T>* out = b;
+    for (int s = 0; s < p.nst; ++s) {
+        const int R = p.R[s], Ns = p.Ns[s];
+        const C2<T>* tw = tab + p.off[s];
+        switch (R) {
+            case 2: mix_stage<T, 2>(in, out, p.L, Ns, tw, nullptr); break;
+            case 4: mix_stage<T, 4>(in, out, p.L, Ns, tw, nullptr); break;
+            case 3: mix_stage<T, 3>(in, out, p.L, Ns, tw, tab + p.root_off[3]); break;
+            case 5: mix_stage<T, 5>(in, out, p.L, Ns, tw, tab + p.root_off[5]); break;
+            default: mix_stage<T, 7>(in, out, p.L, Ns, tw, tab + p.root_off[7]); break;
+        }
+        __syncthreads();
+        C2<T>* t = in;
+        in = out;
+        out = t;
+    }
+    return in;
+}
+
+// ---------------------------------------------------------------------------
 // block reduction helpers
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double block_sum(double x, double* sh) {

@@ -25,7 +25,11 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstdlib>
+#include <map>
+#include <mutex>
 #include <type_traits>
+#include <utility>
+#include <vector>
 
 #include "gb_device.cuh"
 #include "gb_internal.cuh"
@@ -436,6 +440,149 @@ __global__ void cols_direct_kernel(const C2<T>* __restrict__ zt, int N, int band
         out[o] = x;
         if (amp_out) amp_out[o] = cabs_<T>(x);
     }
+}
+
+// ---------------------------------------------------------------------------
+// mixed-radix (2, 3, 4, 5, 7) versions of the row and column passes for even
+// lengths that are not powers of two (block_fft_mixed; ping-pong buffers in
+// shared memory, no padding)
+// ---------------------------------------------------------------------------
+// Row I of the image (or of the swept profile): the M = N/2 complex values
+// x[2m] + i x[2m+1] are transformed and split into the real transform
+// X_k = E_k + exp(-2 pi i k / N) O_k (E, O the transforms of the even and odd
+// samples), k < K.
+template <typename T>
+__global__ void rows_mixed_kernel(const T* __restrict__ image, int N, int row0, const T* __restrict__ intensity, int nr,
+                                  T Rmin, T dR, T dxy, T inv_cos_inc, int rmax, T central, int profile,
+                                  const C2<T>* __restrict__ tw, MixPlan plan, const C2<T>* __restrict__ mtab,
+                                  C2<T>* __restrict__ zt, int host_K, const DevState* __restrict__ st, int row_sign) {
+    using CT = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int M = N / 2;
+    CT* a = reinterpret_cast<CT*>(smem_raw);
+    CT* b = a + M;
+    const int I = row0 + blockIdx.x;
+    const int off = N / 2 - rmax;
+    const T sr_to_px = dxy * dxy;
+    for (int m = threadIdx.x; m < M; m += blockDim.x) {
+        T x[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int J = 2 * m + h;
+            if (profile) {
+                x[h] = sweep_pixel<T>(I, J, intensity, nr, Rmin, dR, (T)1 / dR, dxy, inv_cos_inc, rmax, off, sr_to_px);
+                if (I == N / 2 && J == N / 2) x[h] = central;
+            } else {
+                x[h] = image[(size_t)I * N + J];
+            }
+        }
+        a[m] = CT{x[0], x[1]};
+    }
+    __syncthreads();
+    const CT* Z = block_fft_mixed<T>(a, b, plan, mtab);
+    const int K = get_window(host_K, 0, 0, st).K;
+    const T sgn = (row_sign && (I & 1)) ? (T)-1 : (T)1;
+    const T h = (T)0.5;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+        const CT za = Z[k % M], zb = Z[(M - k % M) % M];
+        const CT e = CT{h * (za.x + zb.x), h * (za.y - zb.y)};
+        const CT o = CT{h * (za.y + zb.y), -h * (za.x - zb.x)};
+        const CT x = cadd(e, cmul(o, __ldg(&tw[k])));
+        zt[(size_t)k * N + I] = CT{sgn * x.x, sgn * x.y};
+    }
+}
+
+// Column k of zt (rows outside [band0, band1) are zero): the length-N
+// transform, window rows written as cols_kernel does
+template <typename T>
+__global__ void cols_mixed_kernel(const C2<T>* __restrict__ zt, int N, int band0, int band1, MixPlan plan,
+                                  const C2<T>* __restrict__ mtab, C2<T>* __restrict__ out, T* __restrict__ amp_out,
+                                  long long s_row, long long s_col, int host_K, int host_r0, int host_W,
+                                  const DevState* __restrict__ st, int out_sign) {
+    using CT = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    CT* a = reinterpret_cast<CT*>(smem_raw);
+    CT* b = a + N;
+    const Window w = get_window(host_K, host_r0, host_W, st);
+    const int k = blockIdx.x;
+    if (k >= w.K) return;  // uniform for the whole block
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+        a[i] = (i >= band0 && i < band1) ? zt[(size_t)k * N + i] : CT{(T)0, (T)0};
+    __syncthreads();
+    const CT* col = block_fft_mixed<T>(a, b, plan, mtab);
+    const int par = (k + N / 2) & 1;
+    for (int q = threadIdx.x; q < w.W; q += blockDim.x) {
+        const int r = w.r0 + q;
+        CT x = col[r];
+        if (out_sign && ((r & 1) ^ par)) x = cneg(x);
+        const long long o = (long long)q * s_row + (long long)k * s_col;
+        out[o] = x;
+        if (amp_out) amp_out[o] = cabs_<T>(x);
+    }
+}
+
+// Plan of a length L = 4^a 2^b 3^c 5^d 7^e (false for other lengths) and its
+// table: per stage, exp(-2 pi i m k / (Ns R)) at off + (m-1) Ns + k, then the
+// R-th roots of unity; long-double values rounded once to T.  Built once per
+// (device, L, precision) and kept until exit.
+bool mix_plan(int L, MixPlan* p) {
+    if (L < 2) return false;
+    MixPlan q{};
+    q.L = L;
+    int n = L, ns = 1, off = 0;
+    for (int r : {4, 2, 3, 5, 7}) {
+        while (n % r == 0) {
+            if (q.nst >= kMixMaxStages) return false;
+            q.R[q.nst] = r;
+            q.Ns[q.nst] = ns;
+            q.off[q.nst] = off;
+            off += (r - 1) * ns;
+            ns *= r;
+            n /= r;
+            ++q.nst;
+        }
+    }
+    if (n != 1) return false;
+    for (int r : {3, 5, 7}) {
+        q.root_off[r] = off;
+        off += r;
+    }
+    *p = q;
+    return true;
+}
+int mix_table_size(const MixPlan& p) { return p.root_off[7] + 7; }
+
+template <typename T> const C2<T>* mix_table(const MixPlan& p) {
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, C2<T>*> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find({dev, p.L});
+    if (it != cache.end()) return it->second;
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    std::vector<C2<T>> h((size_t)mix_table_size(p));
+    for (int s = 0; s < p.nst; ++s) {
+        const int R = p.R[s], Ns = p.Ns[s];
+        for (int m = 1; m < R; ++m)
+            for (int k = 0; k < Ns; ++k) {
+                const long double a = -two_pi * (long double)(m * k) / (long double)(Ns * R);
+                h[(size_t)p.off[s] + (size_t)(m - 1) * Ns + k] = C2<T>{(T)cosl(a), (T)sinl(a)};
+            }
+    }
+    for (int r : {3, 5, 7})
+        for (int j = 0; j < r; ++j) {
+            const long double a = -two_pi * (long double)j / (long double)r;
+            h[(size_t)p.root_off[r] + j] = C2<T>{(T)cosl(a), (T)sinl(a)};
+        }
+    C2<T>* d = nullptr;
+    if (cudaMalloc(&d, sizeof(C2<T>) * h.size()) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(d, h.data(), sizeof(C2<T>) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(d);
+        return nullptr;
+    }
+    cache[{dev, p.L}] = d;
+    return d;
 }
 
 // ---------------------------------------------------------------------------
@@ -1194,6 +1341,16 @@ cudaError_t Launch<T>::rows_image(const T* image, int N, const CT* tw, const CT*
         });
         return e;
     }
+    MixPlan mp;
+    const C2<T>* mt = nullptr;
+    if ((N % 2) == 0 && mix_plan(N / 2, &mp) && sizeof(CT) * (size_t)N <= 200 * 1024 && (mt = mix_table<T>(mp))) {
+        const size_t smm = sizeof(CT) * (size_t)N;  // two buffers of N/2
+        cudaError_t e = set_smem(rows_mixed_kernel<T>, smm);
+        if (e != cudaSuccess) return e;
+        rows_mixed_kernel<T><<<N, 256, smm, s>>>(image, N, 0, nullptr, 0, (T)0, (T)1, (T)1, (T)1, 0, (T)0, 0, tw, mp,
+                                                 mt, zt, host_K, state, row_sign ? 1 : 0);
+        return cudaGetLastError();
+    }
     const size_t sm = sizeof(T) * (size_t)N;
     cudaError_t e = set_smem(rows_direct_kernel<T>, sm);
     if (e != cudaSuccess) return e;
@@ -1244,6 +1401,17 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
             }
         });
         return e;
+    }
+    MixPlan mp;
+    const C2<T>* mt = nullptr;
+    if ((N % 2) == 0 && mix_plan(N / 2, &mp) && sizeof(CT) * (size_t)N <= 200 * 1024 && (mt = mix_table<T>(mp))) {
+        const size_t smm = sizeof(CT) * (size_t)N;
+        cudaError_t e = set_smem(rows_mixed_kernel<T>, smm);
+        if (e != cudaSuccess) return e;
+        rows_mixed_kernel<T><<<nrows, 256, smm, s>>>(nullptr, N, N / 2 - rmax, intensity, nr, (T)Rmin, (T)dR, (T)dxy,
+                                                     inv_cos, rmax, (T)central_value, 1, tw, mp, mt, zt, kcols, state,
+                                                     1);
+        return cudaGetLastError();
     }
     const size_t sm = sizeof(T) * (size_t)N;
     cudaError_t e = set_smem(rows_direct_kernel<T>, sm);
@@ -1315,6 +1483,16 @@ cudaError_t Launch<T>::cols(const CT* zt, int N, int band0, int band1, const CT*
             }
         });
         return e;
+    }
+    MixPlan mp;
+    const C2<T>* mt = nullptr;
+    if (mix_plan(N, &mp) && 2 * sizeof(CT) * (size_t)N <= 200 * 1024 && (mt = mix_table<T>(mp))) {
+        const size_t smm = 2 * sizeof(CT) * (size_t)N;
+        cudaError_t e = set_smem(cols_mixed_kernel<T>, smm);
+        if (e != cudaSuccess) return e;
+        cols_mixed_kernel<T><<<grid, 256, smm, s>>>(zt, N, band0, band1, mp, mt, out, amp_out, s_row, s_col, host_K,
+                                                    host_r0, host_W, state, out_sign ? 1 : 0);
+        return cudaGetLastError();
     }
     const size_t sm = sizeof(CT) * (size_t)N;
     cudaError_t e = set_smem(cols_direct_kernel<T>, sm);

@@ -183,6 +183,31 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
+// 32 accumulator columns of this thread's TMEM lane into r, without waiting:
+// the values are valid after tmem_wait32(r)
+__device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t* r) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+}
+// wait for every outstanding tcgen05.ld of this thread; r passes through the
+// wait so that no use of the loaded values is scheduled before it
+__device__ __forceinline__ void tmem_wait32(uint32_t* r) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                   "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
+                   "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+                 :
+                 : "memory");
+}
+
 // 16 consecutive accumulator columns of this thread's TMEM lane
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
     uint32_t r[16];
@@ -329,12 +354,14 @@ __global__ void __launch_bounds__(kThreads, 1)
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t tx = tmem + lane_off + (uint32_t)(j * 2 * BN), ty = tx + (uint32_t)BN;
 #pragma unroll
-            for (int c0 = 0; c0 < BN; c0 += 16) {
-                float x[16], y[16];
-                tmem_ld16(tx + (uint32_t)c0, x);
-                tmem_ld16(ty + (uint32_t)c0, y);
+            for (int c0 = 0; c0 < BN; c0 += 32) {
+                uint32_t x[32], y[32];
+                tmem_ld32_async(tx + (uint32_t)c0, x);
+                tmem_ld32_async(ty + (uint32_t)c0, y);
+                tmem_wait32(x);
+                tmem_wait32(y);
 #pragma unroll
-                for (int i = 0; i < 16; ++i) acc[c0 + i] += x[i] + y[i];
+                for (int i = 0; i < 32; ++i) acc[c0 + i] += __uint_as_float(x[i]) + __uint_as_float(y[i]);
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             mbar_arrive(&acce[j]);

@@ -129,6 +129,39 @@ def test_profile_wider_than_image(g, orc, nxy):
     assert abs(cg - co) / abs(co) <= DP_CHI2
 
 
+@pytest.mark.parametrize("n", [250, 360, 1000, 6000])
+@pytest.mark.parametrize("prec", ["double", "single"])
+def test_fft2d_mixed_radix_sizes(g, n, prec):
+    """Even sizes that are not powers of two (250 = 2 5^3, 360 = 2^3 3^2 5,
+    1000 = 2^3 5^3, 6000 = 2^4 3 5^3): the mixed-radix (2, 3, 4, 5, 7)
+    shared-memory FFT of the row and column passes, against numpy's rfft2."""
+    mod = getattr(g, prec)
+    rng = np.random.default_rng(n + 7)
+    img = rng.standard_normal((n, n)).astype(mod.real_dtype)
+    ref = np.fft.rfft2(img.astype(np.float64))
+    out = mod._fft2d(img)
+    assert out.shape == (n, n // 2 + 1)
+    tol = 1e-14 if prec == "double" else 4e-6
+    assert rel_max(out, ref) <= tol, rel_max(out, ref)
+
+
+@pytest.mark.parametrize("nxy", [360, 1000])
+def test_chi2_image_mixed_radix_sizes(g, orc, nxy):
+    """chi2Image and sampleImage end to end at non-power-of-two sizes against the oracle."""
+    dxy = 0.01 * arcsec * 1024 / nxy
+    img = _ring_image(nxy, dxy)
+    duv = 1 / (nxy * dxy)
+    u, v = uv_log_uniform(20000, 0.5 * duv, 0.45 * nxy / 2 * duv, seed=nxy)
+    re, im, w = _obs(20000, seed=nxy + 1)
+    kw = dict(dRA=0.02 * arcsec, dDec=-0.01 * arcsec, PA=0.7)
+    vg = g.double.sampleImage(img, dxy, u, v, **kw)
+    vo = orc["double"].sampleImage(img, dxy, u, v, **kw)
+    assert rel_max(vg, vo) <= DP_V
+    cg = g.double.chi2Image(img, dxy, u, v, re, im, w, **kw)
+    co = orc["double"].chi2Image(img, dxy, u, v, re, im, w, **kw)
+    assert abs(cg - co) / abs(co) <= DP_CHI2
+
+
 def test_sweep_double(g, orc):
     Rmin, dR, nr = 1e-6 * arcsec, 0.001 * arcsec, 2000
     dxy = 0.2 * arcsec
