@@ -116,7 +116,10 @@ def chi2_profile_batch(dataset: Dataset, intensity, params, Rmin, dR, dxy, nxy, 
     """chi2 of B profile models against ``dataset``.
 
     intensity: (B, nr) float32 CUDA tensor [Jy/sr] on R = Rmin + i dR;
-    params: (B, 4) float32 CUDA tensor of (inc, PA, dRA, dDec) [rad].
+    params: (B, 4) float32 CUDA tensor of (inc, PA, dRA, dDec) [rad];
+    nxy: even, in [16, 16384]; a power of two unless the spectrum passes run
+    on the tensor cores (the default where the folded quadrant rmax + 1, the
+    uv window and the profile fit them).
     Returns chi2 float64, (B,) summed over the dataset's sets or (B, nsets)
     with per_set=True; with grad=True also dchi2/dintensity (B, nr) and
     dchi2/dparams (B, 4) of the total chi2, both float32.

@@ -1442,15 +1442,17 @@ Shape default_shape(const Geo& g) {
     return sh;
 }
 // a cached shape is used only if every field is one of the current candidates
-bool shape_valid(const Geo& g, const Shape& sh, bool real, bool tma_ok) {
+// (the tensor-core passes use only the visibility pass's field)
+bool shape_valid(const Geo& g, const Shape& sh, bool real, bool tma_ok, bool tc) {
     auto in = [](int x, const std::vector<int>& c) {
         for (int y : c)
             if (y == x) return true;
         return false;
     };
+    const std::vector<int> pts = real ? std::vector<int>{2, 4, 8} : std::vector<int>{2, 4};
+    if (tc) return in(sh.pts, pts);
     const std::vector<int> rows = fft_candidates(g.M), cols = fft_candidates(g.N);
     const bool col_ok = in(sh.e_cols, cols) || (tma_ok && sh.e_cols >= kTmaCols && in(sh.e_cols - kTmaCols, cols));
-    const std::vector<int> pts = real ? std::vector<int>{2, 4, 8} : std::vector<int>{2, 4};
     return in(sh.e_rows, rows) && col_ok && in(sh.e_colsT, cols) && in(sh.e_rowsT, rows) && in(sh.pts, pts);
 }
 bool graphs_enabled() {
@@ -2063,8 +2065,7 @@ static void batch_run(const BatchCall& call) {
         if (nxy < 2 || (nxy & 1))
             throw Err{GALARIO_EINVAL, "Error in check input image: x dimension = " + std::to_string(nxy) +
                                           (nxy < 2 ? " is less than 2" : " is odd")};
-        if (!is_pow2(nxy) || nxy < 16 || nxy > 16384)
-            throw Err{GALARIO_EINVAL, "Error in batch: nxy must be a power of two in [16, 16384]"};
+        if (nxy < 16 || nxy > 16384) throw Err{GALARIO_EINVAL, "Error in batch: nxy must lie in [16, 16384]"};
         if (!image) {
             const double ratio = ((double)dxy / 2. - (double)Rmin) / (double)dR;
             if (ratio < 5)
@@ -2177,6 +2178,10 @@ static void batch_run(const BatchCall& call) {
         const int nF = g.rmax + 1;
         const bool use_tc = real && tc_enabled() && tc::encode_fn() != nullptr && nF <= 2048 && g.K <= 2048 &&
                             g.W <= 4096 && (size_t)nr * sizeof(float) <= 160 * 1024;
+        // the FFT passes need a power of two; the cosine-matrix products take any even nxy
+        if (!use_tc && !is_pow2(nxy))
+            throw Err{GALARIO_EINVAL, std::string("Error in batch: nxy must be a power of two in [16, 16384]") +
+                                          (image ? "" : " (profiles on the tensor-core passes take any even nxy)")};
         const CosMats* cm = use_tc ? &ws.cos_mats(g.N, g.K, g.r0, g.W, g.rmax) : nullptr;
         float *tF = nullptr, *tD1 = nullptr, *tG = nullptr, *tG1 = nullptr, *tGF = nullptr, *tPart = nullptr;
         double* tPinc = nullptr;
@@ -2444,7 +2449,7 @@ static void batch_run(const BatchCall& call) {
                                (fkey = tune_file_key(g.N, g.K, g.W, g.R, B, d->nd_pad, grad ? 1 : 0, nr,
                                                       image ? 1 : (use_tc ? 2 : 0)),
                                 tune_file().lookup(fkey, &fsh)) &&
-                               shape_valid(g, fsh, real, tma_ok);
+                               shape_valid(g, fsh, real, tma_ok, use_tc);
         if (tuned) {
             sh = it->second;
         } else if (from_file) {

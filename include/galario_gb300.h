@@ -232,7 +232,10 @@ int galario_dataset_nsets(void *handle, int *nsets);
  *  grad_intensity (B x nr) and grad_params (B x 4), both or neither (NULL):
  *  d(total chi2)/d(intensity, params).
  * Geometry rules as chi2Profile (galario.cpp:101-121 checks), with nxy a
- * power of two in [16, 16384].  Arithmetic: FP32 FFTs and interpolation;
+ * power of two in [16, 16384], or any even nxy in that range when the
+ * spectrum passes run on the tensor cores (profiles with rmax+1 <= 2048,
+ * K <= 2048, W <= 4096, nr <= 40960; GALARIO_TC=0 turns them off).
+ * Arithmetic: FP32 FFTs and interpolation;
  * uv rotation, cell index and phase in double-float; chi2 and the parameter
  * gradients accumulated in double.  Calls on one device share a workspace
  * and are serialised by a lock. */

@@ -293,3 +293,46 @@ def test_batch_profile_wider_than_image(oracle_port):
         ref = orc.chi2Profile(I[b], f(Rmin), f(dR), nxy, f(dxy), c["u"], c["v"], c["re"], c["im"], c["w"], inc=inc,
                               PA=PA, dRA=dRA, dDec=dDec)
         assert abs(chi2[b] - ref) / ref <= CHI2_TOL, (b, chi2[b], ref)
+
+
+@pytest.mark.parametrize("nxy", [1000, 1536])
+def test_batch_non_power_of_two_nxy(nxy, oracle_port, monkeypatch):
+    """Swept profiles at an even nxy that is not a power of two: the spectrum
+    passes are products with cosine matrices, where nxy enters only the
+    angles.  chi2 against the FP64 oracle, the gradient against the float64
+    torch reference; with the tensor-core passes off (FFT passes, powers of two
+    only) the call is refused, and so is a batch of images at that size."""
+    import torch
+    from galario_gb300.batch import Dataset, chi2_image_batch, chi2_profile_batch, status
+    c = _setup(seed=3, nxy=nxy, nd=30000, B=2)
+    f = np.float32
+    for k in ("u", "v", "re", "im", "w", "I", "params"):
+        c[k] = c[k].astype(f).astype(np.float64)
+    ds = Dataset(c["u"], c["v"], c["re"], c["im"], c["w"])
+    tI = torch.tensor(c["I"], dtype=torch.float32, device="cuda")
+    tp = torch.tensor(c["params"], dtype=torch.float32, device="cuda")
+    args = (c["Rmin"], c["dR"], c["dxy"], nxy)
+    chi2, gI, gp = chi2_profile_batch(ds, tI, tp, *args, grad=True)
+    chi2_fwd = chi2_profile_batch(ds, tI, tp, *args).cpu().numpy()
+    assert status() == 0
+    chi2, gI, gp = chi2.cpu().numpy(), gI.cpu().numpy(), gp.cpu().numpy()
+    orc = oracle_port.get("port", "double")
+    for b in range(2):
+        inc, PA, dRA, dDec = c["params"][b]
+        ref = orc.chi2Profile(c["I"][b], c["Rmin"], c["dR"], nxy, c["dxy"], c["u"], c["v"], c["re"], c["im"],
+                              c["w"], inc=inc, PA=PA, dRA=dRA, dDec=dDec)
+        assert abs(chi2_fwd[b] - ref) / ref <= CHI2_TOL, (b, chi2_fwd[b], ref)
+        assert abs(chi2[b] - ref) / ref <= CHI2_TOL, (b, chi2[b], ref)
+        ref_chi2, ref_gI, ref_gp = _ref_grad(dict(c, nxy=nxy), b)
+        assert abs(ref_chi2 - ref) / ref <= 1e-12
+        assert _rel(gI[b], ref_gI) <= GRAD_SAMPLES_TOL, (b, _rel(gI[b], ref_gI))
+        for a in range(4):
+            assert abs(gp[b, a] - ref_gp[a]) <= GRAD_TOL * abs(ref_gp[a]) + 1e-6 * np.abs(ref_gp).max(), \
+                (b, a, gp[b, a], ref_gp[a])
+    monkeypatch.setenv("GALARIO_TC", "0")
+    with pytest.raises(ValueError, match="power of two"):
+        chi2_profile_batch(ds, tI, tp, *args)
+    monkeypatch.delenv("GALARIO_TC")
+    imgs = torch.zeros((1, nxy, nxy), dtype=torch.float32, device="cuda")
+    with pytest.raises(ValueError, match="power of two"):
+        chi2_image_batch(ds, imgs, torch.zeros((1, 3), dtype=torch.float32, device="cuda"), c["dxy"])
