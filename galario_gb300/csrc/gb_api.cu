@@ -13,6 +13,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <algorithm>
 #include <functional>
@@ -131,6 +132,9 @@ struct Ctx {
     std::map<std::pair<int, int>, void*> tw;   // (N, sizeof(T)) -> table
     std::map<std::pair<int, int>, void*> stw;  // (L * 32 + E, sizeof(T)) -> stage twiddles
     DevState* host_state = nullptr;           // pinned mirror of DevState
+    // the device reads pageable host memory coherently (address translation
+    // services, e.g. NVLink-C2C on Grace): kernels can read the caller's arrays
+    bool host_readable = false;
     // optional per-stage CUDA-event timing (galario_stage_timing)
     bool timing = false;
     struct Rec {
@@ -162,6 +166,9 @@ struct Ctx {
         CK(cudaEventCreateWithFlags(&ev_vis2, cudaEventDisableTiming));
         for (auto& e : ev_chunk) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         CK(cudaMallocHost(&host_state, sizeof(DevState)));
+        int pageable = 0;
+        CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
+        host_readable = pageable != 0;
         // exp(2 pi i j / T), j in [0, T), as exp(2 pi i jh / 2^10) exp(2 pi i jl / T)
         // with j = 2^10 jh + jl: the two factors of 2^10 entries each from long
         // double, kept as double-double pairs, multiplied in double-double
@@ -284,6 +291,26 @@ const char* const kStageNames[ST_COUNT] = {"h2d", "extent", "rows", "cols", "vis
 
 template <typename T> T* as(DevBuf& b, size_t count) { return static_cast<T*>(b.get(sizeof(T) * count)); }
 
+// Host-pointer chi2 calls read the caller's arrays from the kernels where the
+// device can (GALARIO_ZERO_COPY=0 keeps the copy-engine uploads).
+bool zero_copy(const Ctx& c) {
+    const char* v = std::getenv("GALARIO_ZERO_COPY");
+    return c.host_readable && !(v && v[0] == '0');
+}
+// visibilities whose observations the staged schedule copies ahead (while
+// the column pass runs); the rest are read in place by the visibility pass
+inline int staged_head(int nd) { return std::min(nd / 4, 3 << 17) & ~255; }
+// page-locked (or registered) host memory: the copy engines read it without
+// blocking the host
+bool is_pinned(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 void h2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
     if (bytes) CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
 }
@@ -369,6 +396,15 @@ struct Overlap {
     cudaEvent_t ev_uv = nullptr;
     int nchunks = 1;
     const cudaEvent_t* ev_chunk = nullptr;
+    // Staged mode (a device that reads host memory directly): the pass that
+    // copied (u, v) to the device also computed the extent; visibilities
+    // [0, n0) have their (Re, Im, w) copied to re0/im0/w0 (ready at
+    // ev_chunk[0]) and [n0, nd) are read from the caller's arrays by the
+    // visibility pass itself.
+    bool staged = false;
+    bool extent_done = false;  // the staging pass computed the extent (else the pipeline runs it after ev_uv)
+    int n0 = 0;
+    const void *re0 = nullptr, *im0 = nullptr, *w0 = nullptr;
 };
 // chunk c of nd visibilities in n chunks: [chunk_begin(nd, n, c), chunk_begin(nd, n, c + 1))
 // (equal sizes: chunks falling in size, so that less is left after the last
@@ -395,9 +431,16 @@ template <typename T> struct Pipe {
         const long long qcap = std::min<long long>((long long)C * N, QUAD_CAP);
         T* quads = as<T>(c.quad, (size_t)qcap * QUAD_REC);
         const int nchunks = (ov && nd > 0) ? ov->nchunks : 1;
+        const bool staged = ov && ov->staged && nd > 0;
+        // visibility ranges of the launches: staged, [0, n0) and [n0, nd); else the chunks
+        std::vector<std::pair<int, int>> ranges;
+        if (staged) {
+            ranges.emplace_back(0, nd);
+        } else {
+            for (int k = 0; k < nchunks; ++k) ranges.emplace_back(chunk_begin(nd, nchunks, k), chunk_begin(nd, nchunks, k + 1));
+        }
         size_t nparts = 0;
-        for (int k = 0; k < nchunks; ++k)
-            nparts += (size_t)L::vis_grid(std::max(1, chunk_begin(nd, nchunks, k + 1) - chunk_begin(nd, nchunks, k)));
+        for (const auto& r : ranges) nparts += (size_t)L::vis_grid(std::max(1, r.second - r.first));
         double* partials = as<double>(c.partials, nparts);
         if (!have_extent && !ov) timed(c, s, ST_EXTENT, [&] { CK(L::extent(u, v, nd, N, duv, st, s)); });
         int band0 = 0, band1 = N;
@@ -419,7 +462,7 @@ template <typename T> struct Pipe {
         }
         if (ov) {
             CK(cudaStreamWaitEvent(s, ov->ev_uv, 0));
-            timed(c, s, ST_EXTENT, [&] { CK(L::extent(u, v, nd, N, duv, st, s)); });
+            if (!ov->extent_done) timed(c, s, ST_EXTENT, [&] { CK(L::extent(u, v, nd, N, duv, st, s)); });
         }
         // window layout: column k at win + k*N, rows [r0, r0+W) contiguous
         timed(c, s, ST_COLS, [&] {
@@ -474,7 +517,19 @@ template <typename T> struct Pipe {
         a.chi2_out = chi2_out;
         a.state = st;
         if (before_vis) before_vis();
-        if (nd > 0 && ov) {
+        if (staged) {
+            // one launch: the first n0 visibilities' observations from their
+            // device copies (ready at ev_chunk[0]), the rest read in place
+            a.re = static_cast<const T*>(ov->re0);
+            a.im = static_cast<const T*>(ov->im0);
+            a.w = static_cast<const T*>(ov->w0);
+            a.re2 = re;
+            a.im2 = im;
+            a.w2 = w;
+            a.split = ov->n0;
+            CK(cudaStreamWaitEvent(s, ov->ev_chunk[0], 0));
+            timed(c, s, ST_VIS, [&] { CK(L::vis(a, s)); });
+        } else if (nd > 0 && ov) {
             int total = 0;
             for (int k = 0; k < nchunks; ++k)
                 total += L::vis_grid(std::max(1, chunk_begin(nd, nchunks, k + 1) - chunk_begin(nd, nchunks, k)));
@@ -639,6 +694,46 @@ template <typename T> struct Api {
         // only the profile) runs on `s`
         timed(c, s, ST_H2D, [&] { h2d(I_d, I, sizeof(T) * (size_t)nr, s); });
         CK(cudaMemsetAsync(st, 0, sizeof(DevState), s));
+        if (zero_copy(c) && nd > 0) {
+            // Staged schedule: the side stream's extent pass reads (u, v)
+            // from the caller's arrays, writes their device copies and the
+            // window; then the observations of the first visibilities are
+            // copied while the row and column passes run; the visibility
+            // pass reads the rest in place.  Kernel launches only: the host
+            // never blocks on a pageable copy.
+            Overlap ov;
+            ov.ev_uv = c.ev_uv;
+            ov.ev_chunk = c.ev_chunk;
+            ov.staged = true;
+            ov.n0 = staged_head(nd);
+            ov.re0 = re_d;
+            ov.im0 = im_d;
+            ov.w0 = w_d;
+            CK(cudaEventRecord(c.ev_side_start, s));
+            CK(cudaStreamWaitEvent(c.side, c.ev_side_start, 0));
+            const bool pinned = is_pinned(u) && is_pinned(v) && is_pinned(re) && is_pinned(im) && is_pinned(w);
+            if (pinned) {
+                // copy engines: the SMs stay free for the row pass
+                h2d(u_d, u, sizeof(T) * (size_t)nd, c.side);
+                h2d(v_d, v, sizeof(T) * (size_t)nd, c.side);
+                CK(cudaEventRecord(c.ev_uv, c.side));
+                h2d(re_d, re, sizeof(T) * (size_t)ov.n0, c.side);
+                h2d(im_d, im, sizeof(T) * (size_t)ov.n0, c.side);
+                h2d(w_d, w, sizeof(T) * (size_t)ov.n0, c.side);
+            } else {
+                // a pageable copy would block the host: kernels read the arrays
+                CK(L::extent(u, v, nd, N, (double)duv, st, c.side, u_d, v_d));
+                CK(cudaEventRecord(c.ev_uv, c.side));
+                ov.extent_done = true;
+                CK(L::stage3(re, im, w, re_d, im_d, w_d, ov.n0, c.side));
+            }
+            CK(cudaEventRecord(c.ev_chunk[0], c.side));
+            Pipe<T>::enqueue(c, s, N, (double)duv, nullptr, I_d, nr, Rmin, dR, dxy, inc, &pg, 1.0, dRA, dDec, PA, nd,
+                             u_d, v_d, re, im, w, nullptr, true, nullptr, st, false, std::function<void()>(), &ov);
+            finish(c, st);
+            *chi2 = (T)c.host_state->chi2;
+            return;
+        }
         Overlap ov;
         ov.ev_uv = c.ev_uv;
         ov.nchunks = std::max(1, std::min(Ctx::kMaxChunks, nd >> 18));

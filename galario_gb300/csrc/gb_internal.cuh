@@ -90,8 +90,13 @@ inline bool is_pow2(long long n) { return n > 0 && (n & (n - 1)) == 0; }
 template <typename T> struct Launch {
     using CT = C2<T>;
     // dataset extent: state->rmax2 = max(u^2 + v^2)
-    // ... and the window (state->win_*) derived from it for an N x N image with cell duv
-    static cudaError_t extent(const T* u, const T* v, int nd, int N, double duv, DevState* state, cudaStream_t s);
+    // ... and the window (state->win_*) derived from it for an N x N image with cell duv.
+    // u_out, v_out (both or neither): also copy u, v there (u, v may then be
+    // host memory the device reads directly)
+    static cudaError_t extent(const T* u, const T* v, int nd, int N, double duv, DevState* state, cudaStream_t s,
+                              T* u_out = nullptr, T* v_out = nullptr);
+    // copy [0, n) of a, b, c into da, db, dc (the sources may be host memory the device reads directly)
+    static cudaError_t stage3(const T* a, const T* b, const T* c, T* da, T* db, T* dc, int n, cudaStream_t s);
     // row pass on an image (rows [0, N)), output zt for columns [0, K) where
     // K = host_K if >= 0, else from state->rmax2 (window_from_extent).
     // row_sign: multiply row i by (-1)^i.
@@ -174,6 +179,11 @@ template <typename T> struct Launch {
             ddec_df = split(ddec);
         }
         const T *u, *v, *re, *im, *w;
+        // observations of visibilities [split, nd) come from re2/im2/w2 (same
+        // indexing) instead: the caller's host arrays, read in place, when
+        // re/im/w hold device copies of the first `split` only
+        const T *re2 = nullptr, *im2 = nullptr, *w2 = nullptr;
+        int split = 0x7fffffff;
         int nd;
         CT* vis_out;         // may be null
         double* partials;    // chi2 partials (null: no chi2)

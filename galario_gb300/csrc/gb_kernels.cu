@@ -603,16 +603,19 @@ __device__ __forceinline__ float abs_bound_f(double x) {
 
 template <typename T>
 __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, int nd, int N, double duv,
-                              DevState* st) {
+                              DevState* st, T* __restrict__ u_out, T* __restrict__ v_out) {
     // max(u^2 + v^2) (NaN entries are ignored here and flagged by the
     // visibility pass), in FP32: for FP64 inputs as the sum of squares of
     // upper bounds of |u| and |v| (an upper bound itself: its rounding is far
     // below the bounds' slack); the window adds a relative margin larger than
-    // the slack
+    // the slack.  With u_out and v_out (both or neither) the pass also writes
+    // a copy of u and v there: it stages arrays that sit in host memory.
+    const bool copy = u_out != nullptr;
     float mt = 0.f;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     int done = 0;
-    if ((reinterpret_cast<uintptr_t>(u) & 15) == 0 && (reinterpret_cast<uintptr_t>(v) & 15) == 0) {
+    if ((reinterpret_cast<uintptr_t>(u) & 15) == 0 && (reinterpret_cast<uintptr_t>(v) & 15) == 0 &&
+        (reinterpret_cast<uintptr_t>(u_out) & 15) == 0 && (reinterpret_cast<uintptr_t>(v_out) & 15) == 0) {
         // 16-byte vector loads
         using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
         constexpr int L = 16 / sizeof(T);
@@ -639,12 +642,30 @@ __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, 
             }
 #pragma unroll
             for (int r = 0; r < 4; ++r) acc(a[r], b[r]);
+            if (copy) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    reinterpret_cast<V*>(u_out)[i + r * nth] = a[r];
+                    reinterpret_cast<V*>(v_out)[i + r * nth] = b[r];
+                }
+            }
         }
-        for (; i < nvec; i += nth) acc(__ldg(&uv[i]), __ldg(&vv[i]));
+        for (; i < nvec; i += nth) {
+            const V a = __ldg(&uv[i]), b = __ldg(&vv[i]);
+            acc(a, b);
+            if (copy) {
+                reinterpret_cast<V*>(u_out)[i] = a;
+                reinterpret_cast<V*>(v_out)[i] = b;
+            }
+        }
         done = nvec * L;
     }
     for (int i = done + tid; i < nd; i += nth) {
         const T a = __ldg(&u[i]), b = __ldg(&v[i]);
+        if (copy) {
+            u_out[i] = a;
+            v_out[i] = b;
+        }
         if constexpr (sizeof(T) == 4) {
             mt = fmaxf(mt, a * a + b * b);
         } else {
@@ -673,6 +694,38 @@ __global__ void extent_kernel(const T* __restrict__ u, const T* __restrict__ v, 
             st->win_W = w.W;
             st->ticket_extent = 0u;
         }
+    }
+}
+
+// Copy of [0, n) of three arrays (the observations' first visibilities, read
+// from host memory) into device buffers; three 16-byte loads in flight per
+// thread where all six pointers allow vectors.
+template <typename T>
+__global__ void stage3_kernel(const T* __restrict__ a, const T* __restrict__ b, const T* __restrict__ c,
+                              T* __restrict__ da, T* __restrict__ db, T* __restrict__ dc, int n) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    int done = 0;
+    const uintptr_t al = reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) |
+                         reinterpret_cast<uintptr_t>(c) | reinterpret_cast<uintptr_t>(da) |
+                         reinterpret_cast<uintptr_t>(db) | reinterpret_cast<uintptr_t>(dc);
+    if ((al & 15) == 0) {
+        using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+        constexpr int L = 16 / sizeof(T);
+        const int nvec = n / L;
+        for (int i = tid; i < nvec; i += nth) {
+            const V x = __ldg(reinterpret_cast<const V*>(a) + i);
+            const V y = __ldg(reinterpret_cast<const V*>(b) + i);
+            const V z = __ldg(reinterpret_cast<const V*>(c) + i);
+            reinterpret_cast<V*>(da)[i] = x;
+            reinterpret_cast<V*>(db)[i] = y;
+            reinterpret_cast<V*>(dc)[i] = z;
+        }
+        done = nvec * L;
+    }
+    for (int i = done + tid; i < n; i += nth) {
+        da[i] = __ldg(&a[i]);
+        db[i] = __ldg(&b[i]);
+        dc[i] = __ldg(&c[i]);
     }
 }
 
@@ -1028,7 +1081,8 @@ __device__ __forceinline__ C2<T> vis_point(const typename Launch<T>::VisArgs& a,
 
 // Grid-stride over the visibilities, two independent points per iteration so
 // their load -> gather chains overlap.
-template <typename T, bool CHI2, bool VISOUT, bool REALQ>
+// SPLIT: the observations of visibilities [a.split, nd) come from re2/im2/w2.
+template <typename T, bool CHI2, bool VISOUT, bool REALQ, bool SPLIT = false>
 __global__ void __launch_bounds__(256, (sizeof(T) == 8 && REALQ) ? 4 : 1) vis_kernel(typename Launch<T>::VisArgs a) {
     using CT = C2<T>;
     __shared__ double sh[32];
@@ -1044,13 +1098,14 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 8 && REALQ) ? 4 : 1) vis_ke
         const T u1 = has1 ? __ldg(&a.u[i1]) : (T)0, v1 = has1 ? __ldg(&a.v[i1]) : (T)0;
         T re0 = (T)0, im0 = (T)0, w0 = (T)0, re1 = (T)0, im1 = (T)0, w1 = (T)0;
         if (CHI2) {
-            re0 = __ldg(&a.re[i0]);
-            im0 = __ldg(&a.im[i0]);
-            w0 = __ldg(&a.w[i0]);
+            const bool h0 = SPLIT && i0 >= a.split, h1 = SPLIT && i1 >= a.split;
+            re0 = __ldg(&(h0 ? a.re2 : a.re)[i0]);
+            im0 = __ldg(&(h0 ? a.im2 : a.im)[i0]);
+            w0 = __ldg(&(h0 ? a.w2 : a.w)[i0]);
             if (has1) {
-                re1 = __ldg(&a.re[i1]);
-                im1 = __ldg(&a.im[i1]);
-                w1 = __ldg(&a.w[i1]);
+                re1 = __ldg(&(h1 ? a.re2 : a.re)[i1]);
+                im1 = __ldg(&(h1 ? a.im2 : a.im)[i1]);
+                w1 = __ldg(&(h1 ? a.w2 : a.w)[i1]);
             }
         }
         unsigned e0 = 0u, e1 = 0u;
@@ -1269,12 +1324,35 @@ bool rows_tma_enabled() {
 }
 
 template <typename T>
-cudaError_t Launch<T>::extent(const T* u, const T* v, int nd, int N, double duv, DevState* state, cudaStream_t s) {
-    int blocks = (nd + 255) / 256;
-    const int cap = num_sms() * 8;
+cudaError_t Launch<T>::extent(const T* u, const T* v, int nd, int N, double duv, DevState* state, cudaStream_t s,
+                              T* u_out, T* v_out) {
+    if ((u_out == nullptr) != (v_out == nullptr)) return cudaErrorInvalidValue;
+    const int threads = u_out ? 128 : 256;
+    int blocks = (nd + threads - 1) / threads;
+    // staging from host memory: one CTA per SM keeps enough loads in flight
+    // to fill the host link and leaves the SMs to the row pass beside it
+    const int cap = num_sms() * (u_out ? 1 : 8);
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    extent_kernel<T><<<blocks, 256, 0, s>>>(u, v, nd, N, duv, state);
+    // an SM changes its L1/shared split only when idle: ask for the largest
+    // shared share, so that the row pass's blocks fit beside these
+    cudaError_t e = cudaFuncSetAttribute(extent_kernel<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+    extent_kernel<T><<<blocks, threads, 0, s>>>(u, v, nd, N, duv, state, u_out, v_out);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Launch<T>::stage3(const T* a, const T* b, const T* c, T* da, T* db, T* dc, int n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    int blocks = (n + 255) / 256;
+    const int cap = num_sms();
+    if (blocks > cap) blocks = cap;
+    cudaError_t e = cudaFuncSetAttribute(stage3_kernel<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+    stage3_kernel<T><<<blocks, 128, 0, s>>>(a, b, c, da, db, dc, n);
     return cudaGetLastError();
 }
 
@@ -1517,6 +1595,12 @@ template <typename T> cudaError_t Launch<T>::vis(const VisArgs& args, cudaStream
     const bool chi2 = a.partials != nullptr, vo = a.vis_out != nullptr;
     // real_quads: the spectrum of a swept profile, interpolated as a real spectrum
     if (!(chi2 || vo)) return cudaErrorInvalidValue;
+    if (a.split < a.nd) {  // observations partly from re2/im2/w2 (chi2 only)
+        if (!chi2 || vo || !a.re2 || !a.im2 || !a.w2) return cudaErrorInvalidValue;
+        if (a.real_quads && a.quads) vis_kernel<T, true, false, true, true><<<blocks, 256, 0, s>>>(a);
+        else vis_kernel<T, true, false, false, true><<<blocks, 256, 0, s>>>(a);
+        return cudaGetLastError();
+    }
     if (a.real_quads && a.quads) {
         if (chi2 && vo) vis_kernel<T, true, true, true><<<blocks, 256, 0, s>>>(a);
         else if (chi2) vis_kernel<T, true, false, true><<<blocks, 256, 0, s>>>(a);
