@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libgalario_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["gb_kernels.cu", "gb_api.cu", "gb_noalloc.cu", "gb_batch.cu", "gb_probe.cu"]
+SOURCES = ["gb_kernels.cu", "gb_api.cu", "gb_noalloc.cu", "gb_batch.cu", "gb_probe.cu", "gb_profile_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", INCLUDE]
 

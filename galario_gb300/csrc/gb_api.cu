@@ -129,6 +129,11 @@ struct Ctx {
     cudaEvent_t ev_win = nullptr, ev_vis2 = nullptr;
     DevBuf state, partials, img, prof, u, v, re, im, w, vis, zt, win, amp, quad, urot, vrot;
     double2* phase_tab = nullptr;  // table of the FP64 phase shift (PHASE_T entries)
+    ProfileTc* ptc = nullptr;      // tensor-core spectrum of FP64 profiles (created on first use)
+    ProfileTc* profile_tc() {
+        if (!ptc) ptc = profile_tc_new();
+        return ptc;
+    }
     std::map<std::pair<int, int>, void*> tw;   // (N, sizeof(T)) -> table
     std::map<std::pair<int, int>, void*> stw;  // (L * 32 + E, sizeof(T)) -> stage twiddles
     DevState* host_state = nullptr;           // pinned mirror of DevState
@@ -219,6 +224,8 @@ struct Ctx {
         DevBuf* bufs[] = {&state, &partials, &img, &prof, &u, &v, &re, &im, &w, &vis, &zt, &win, &amp, &quad,
                           &urot, &vrot};
         for (DevBuf* b : bufs) b->release();
+        profile_tc_free(ptc);
+        ptc = nullptr;
         for (auto& kv : tw) cudaFree(kv.second);
         tw.clear();
         for (auto& kv : stw) cudaFree(kv.second);
@@ -448,10 +455,22 @@ template <typename T> struct Pipe {
         const CT* stw_cols = c.stage_tw<T>(N);
         // FP64 swept profiles: rows and columns as even-sequence transforms (FFT
         // length N/4); the FP32 passes are faster as paired transforms
-        const CT* stw_q =
-            (!img && sizeof(T) == 8 && even_dft_ok<T>(N)) ? c.stage_tw<T>(N / 4, even_dft_e<T>(N)) : nullptr;
+        // FP64 swept profiles whose quadrant fits the exact level sums: the
+        // window as two cosine-matrix products on the tensor cores
+        // (gb_profile_tc.cu) instead of the row and column transforms
+        const bool tc_prof = !img && sizeof(T) == 8 && profile_tc_ok(N, pg->rmax);
+        const CT* stw_q = (!img && !tc_prof && sizeof(T) == 8 && even_dft_ok<T>(N))
+                              ? c.stage_tw<T>(N / 4, even_dft_e<T>(N))
+                              : nullptr;
         if (img) {
             timed(c, s, ST_ROWS, [&] { CK(L::rows_image(img, N, tw, stw_rows, zt, -1, st, duv, true, s)); });
+        } else if (tc_prof) {
+            if constexpr (sizeof(T) == 8) {
+                timed(c, s, ST_ROWS, [&] {
+                    CK(profile_tc_fold(c.profile_tc(), prof, nr, Rmin, dR, dxy, std::cos(inc), pg->rmax, pg->central,
+                                       N, s));
+                });
+            }
         } else {
             band0 = N / 2 - pg->rmax;
             band1 = N / 2 + pg->rmax;
@@ -466,15 +485,18 @@ template <typename T> struct Pipe {
         }
         // window layout: column k at win + k*N, rows [r0, r0+W) contiguous
         timed(c, s, ST_COLS, [&] {
-            if (img)
+            if (img) {
                 CK(L::cols(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, -1, -1, -1, st, duv, true, s));
-            else
-                CK(L::cols_profile(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, st, duv, s, stw_q, quads, qcap));
+            } else if (tc_prof) {
+                if constexpr (sizeof(T) == 8)
+                    CK(profile_tc_window(c.profile_tc(), N, st, win, amp, 1, N, s));
+            } else {
+                CK(L::cols_profile(zt, N, band0, band1, tw, stw_cols, win, amp, 1, N, st, duv, s, stw_q));
+            }
         });
         // a swept profile's spectrum is real: 4 real corners per cell record
         const bool real_spec = img == nullptr;
         timed(c, s, ST_QUAD, [&] {
-            if (real_spec && stw_q) return;  // the even-sequence column pass wrote the records
             if (real_spec)
                 CK(L::quads_real(win, 1, N, C, st, quads, qcap, s));
             else

@@ -825,5 +825,9 @@ template <typename K> cudaError_t set_smem(K kernel, size_t smem) {
     return cudaSuccess;
 }
 
+// Reals per record of a real spectrum: FP32, the 4 corners; FP64, the 4
+// coefficients of the bilinear modulus and the 4 corners as FP32 (4 floats in
+// the space of 2 doubles; 48-byte records).
+template <typename T> __host__ __device__ constexpr int real_rec() { return sizeof(T) == 8 ? 6 : 4; }
 
 }  // namespace gbg

@@ -119,13 +119,10 @@ template <typename T> struct Launch {
     // column pass of a swept profile (real, even columns): two columns per
     // complex transform; device window; output sign applied
     // stw4 (stage twiddles of length N/4; row pass too): the even-sequence
-    // transform of one column per block, for the N where even_dft_ok holds,
-    // which also writes the real cell records of quads_real into quads (when
-    // the window has at most quad_cap cells); returns whether it did
+    // transform of one column per block, for the N where even_dft_ok holds
     static cudaError_t cols_profile(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
                                     T* amp_out, long long s_row, long long s_col, const DevState* state, double duv,
-                                    cudaStream_t s, const CT* stw4 = nullptr, T* quads = nullptr,
-                                    long long quad_cap = 0);
+                                    cudaStream_t s, const CT* stw4 = nullptr);
     // stw: stage twiddles of the length-N column FFT
     static cudaError_t cols(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
                             T* amp_out, long long s_row, long long s_col, int host_K, int host_r0, int host_W,
@@ -210,8 +207,9 @@ template <typename T> struct Launch {
     static cudaError_t quads(const CT* spec, const T* amp, long long s_row, long long s_col, int C,
                              const DevState* state, T* quads, long long cap, int host_K, int host_r0, int host_W,
                              cudaStream_t s);
-    // records of a real spectrum: the 4 real corners of every cell (4 T per cell;
-    // in FP64 followed by their 4 FP32 copies, 48 bytes per cell)
+    // records of a real spectrum: FP32, the 4 real corners of every cell (16
+    // bytes); FP64, the 4 coefficients of the bilinear modulus and the 4
+    // corners as FP32 (48 bytes; see quad_real_kernel)
     static cudaError_t quads_real(const CT* spec, long long s_row, long long s_col, int C, const DevState* state,
                                   T* quads, long long cap, cudaStream_t s);
     static int vis_grid(int nd);
@@ -229,5 +227,26 @@ template <typename T> struct Launch {
 };
 
 int num_sms();
+
+// ---------------------------------------------------------------------------
+// Spectrum window of a swept FP64 profile as two FP64-grade cosine-matrix
+// products on the tensor cores (gb_profile_tc.cu), per-device state.
+// ---------------------------------------------------------------------------
+struct ProfileTc;
+ProfileTc* profile_tc_new();
+void profile_tc_free(ProfileTc* t);
+// quadrant size of the sweep: columns/rows c < nF of the folded image
+int profile_tc_quadrant(int N, int rmax);
+// the path applies: even N, a quadrant within the exact level sums
+// (nF <= 511), tensor maps available, GALARIO_TC not 0
+bool profile_tc_ok(int N, int rmax);
+// the quadrant of the sweep as digits (independent of the window); prepares
+// the geometry (cosine digits, buffers) on its first call for (N, nF)
+cudaError_t profile_tc_fold(ProfileTc* t, const double* intensity, int nr, double Rmin, double dR, double dxy,
+                            double cos_inc, int rmax, double central, int N, cudaStream_t s);
+// after the extent pass: the window (out, amp: rows [r0, r0+W) of columns
+// [0, K) at q * s_row + k * s_col); errors of bounded waits set ERR_SPIN in st
+cudaError_t profile_tc_window(ProfileTc* t, int N, DevState* st, C2<double>* out, double* amp, long long s_row,
+                              long long s_col, cudaStream_t s);
 
 }  // namespace gbg

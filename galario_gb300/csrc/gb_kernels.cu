@@ -39,10 +39,6 @@ namespace gbg {
 
 namespace {
 
-// Reals per record of a real spectrum: the 4 corners, and in FP64 also their
-// FP32 copies (4 floats in the space of 2 doubles; 48-byte records).
-template <typename T> __host__ __device__ constexpr int real_rec() { return sizeof(T) == 8 ? 6 : 4; }
-
 // ---------------------------------------------------------------------------
 // row pass kernels
 // ---------------------------------------------------------------------------
@@ -304,8 +300,7 @@ __global__ void __launch_bounds__(MAXT) cols_profile_dct_kernel(const C2<T>* __r
                                                                 const C2<T>* __restrict__ tw,
                                                                 const C2<T>* __restrict__ stw4, C2<T>* __restrict__ out,
                                                                 T* __restrict__ amp_out, long long s_row,
-                                                                long long s_col, const DevState* __restrict__ st,
-                                                                T* __restrict__ quads, long long cap) {
+                                                                long long s_col, const DevState* __restrict__ st) {
     using CT = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Window w = get_window(-1, -1, -1, st);
@@ -326,42 +321,12 @@ __global__ void __launch_bounds__(MAXT) cols_profile_dct_kernel(const C2<T>* __r
     const int dmax = max(N / 2 - w.r0, w.r0 + w.W - 1 - N / 2);
     even_dft_block<T, E>(xs, nnz, xn, n, tw, stw4, buf, im, xs, dmax);
     const T ks = (k & 1) ? (T)-1 : (T)1;
-    // the cell records of quad_real_kernel, written here: this column's
-    // element (q, k) is corner y0 of cell (k, q), y1 of (k, q-1), y3 of
-    // (k-1, q) and y2 of (k-1, q-1); with the flat-index wrap of the last
-    // column (K = C), column 0 also gives y3 of cell (C-1, q-1) and y2 of
-    // (C-1, q-2).  A cell (kc, qc) exists for kc + 1 < K, qc + 1 < W, and the
-    // wrapped one (kc = C-1) for qc + 2 < W.
-    const int C = N / 2 + 1;
-    const bool recs = quads && (long long)w.K * w.W <= cap;
-    auto put = [&](int kc, int qc, int corner, T f) {
-        T* rec = quads + ((long long)kc * w.W + qc) * real_rec<T>();
-        rec[corner] = f;
-        if constexpr (sizeof(T) == 8) reinterpret_cast<float*>(rec + 4)[corner] = (float)f;
-    };
     for (int q = threadIdx.x; q < w.W; q += blockDim.x) {
         const int d = abs(w.r0 + q - N / 2);
         const T f = ks * xs[d];
         const long long o = (long long)q * s_row + (long long)k * s_col;
         out[o] = CT{f, (T)0};
         amp_out[o] = fabs(f);
-        if (recs) {
-            if (k + 1 < w.K && k + 1 < C) {  // cells (k, q) and (k, q-1), not wrapped
-                if (q + 1 < w.W) put(k, q, 0, f);
-                if (q >= 1) put(k, q - 1, 1, f);
-            } else if (k + 1 == C && k < w.K) {  // wrapped cells of the last column
-                if (q + 2 < w.W) put(k, q, 0, f);
-                if (q >= 1 && q + 1 < w.W) put(k, q - 1, 1, f);
-            }
-            if (k >= 1 && k < w.K) {  // cells (k-1, q) and (k-1, q-1)
-                if (q + 1 < w.W) put(k - 1, q, 3, f);
-                if (q >= 1) put(k - 1, q - 1, 2, f);
-            }
-            if (k == 0 && w.K == C) {  // column 0 completes the wrapped cells of column C-1
-                if (q >= 1 && q + 1 < w.W) put(C - 1, q - 1, 3, f);
-                if (q >= 2) put(C - 1, q - 2, 2, f);
-            }
-        }
     }
 }
 
@@ -801,6 +766,9 @@ __device__ __forceinline__ bool interp_cell_real(const typename Launch<T>::VisAr
     T yr[4];
     float yf[4];
     bool have_f = false;
+    T amp = (T)0;
+    bool have_amp = false;  // FP64 records: modulus from their coefficients, signed corners from spec if needed
+    bool have_y = false;    // FP32 records: the signed corners
     if ((long long)w.K * w.W <= a.quad_cap) {
         const bool inside = wrap ? (w.K == C && qq >= 0 && qq < w.W - 2) : (c0 < w.K - 1 && qq >= 0 && qq < w.W - 1);
         if (!inside) {
@@ -814,40 +782,48 @@ __device__ __forceinline__ bool interp_cell_real(const typename Launch<T>::VisAr
             yr[1] = p0.y;
             yr[2] = p0.z;
             yr[3] = p0.w;
+            have_y = true;
         } else {
+            // the reference's bilinear modulus (interpolate_core :804-812) from
+            // the record's coefficients (see quad_real_kernel)
             const double2 p0 = __ldg(reinterpret_cast<const double2*>(rec));
             const double2 p1 = __ldg(reinterpret_cast<const double2*>(rec) + 1);
             const float4 pf = __ldg(reinterpret_cast<const float4*>(rec + 4));
-            yr[0] = p0.x;
-            yr[1] = p0.y;
-            yr[2] = p1.x;
-            yr[3] = p1.y;
+            amp = fma(q, fma(t, p1.y, p1.x), fma(t, p0.y, p0.x));
+            have_amp = true;
             yf[0] = pf.x;
             yf[1] = pf.y;
             yf[2] = pf.z;
             yf[3] = pf.w;
             have_f = true;
         }
-    } else {
+    }
+    // the four signed corners from the window (cells without a record, and
+    // FP64 cells whose sign the FP32 estimate leaves open)
+    auto corners = [&]() -> bool {
         const int rr[4] = {r0, r0 + 1, r_last, wrap ? r0 + 1 : r0};
         const int cc[4] = {c0, c0, wrap ? 0 : c0 + 1, wrap ? 0 : c0 + 1};
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             const int qc = rr[c] - w.r0;
-            if (cc[c] >= w.K || qc < 0 || qc >= w.W) {
-                *err |= ERR_WINDOW;
-                return false;
-            }
+            if (cc[c] >= w.K || qc < 0 || qc >= w.W) return false;
             yr[c] = __ldg(&a.spec[(long long)qc * a.s_row + (long long)cc[c] * a.s_col]).x;
         }
+        return true;
+    };
+    if (!have_amp && !have_y && !corners()) {
+        *err |= ERR_WINDOW;
+        return false;
     }
     // the reference's bilinear forms (interpolate_core :782-812),
     // y0 + t (y1 - y0) + q ((y3 - y0) + t (y0 - y1 + y2 - y3)), in fused
     // multiply-adds: the moduli, and the signed corners z of which only the
     // sign is used
-    const T m0 = fabs(yr[0]), m1 = fabs(yr[1]), m2 = fabs(yr[2]), m3 = fabs(yr[3]);
-    const T e1 = m1 - m0, e3 = m3 - m0;
-    const T amp = fma(q, fma(t, (m2 - m3) - e1, e3), fma(t, e1, m0));
+    if (!have_amp) {
+        const T m0 = fabs(yr[0]), m1 = fabs(yr[1]), m2 = fabs(yr[2]), m3 = fabs(yr[3]);
+        const T e1 = m1 - m0, e3 = m3 - m0;
+        amp = fma(q, fma(t, (m2 - m3) - e1, e3), fma(t, e1, m0));
+    }
     bool neg;
     bool decided = false;
     if constexpr (sizeof(T) == 8) {
@@ -867,6 +843,10 @@ __device__ __forceinline__ bool interp_cell_real(const typename Launch<T>::VisAr
         }
     }
     if (!decided) {
+        if (have_amp && !corners()) {
+            *err |= ERR_WINDOW;
+            return false;
+        }
         const T f1 = yr[1] - yr[0], f3 = yr[3] - yr[0];
         const T zr = fma(q, fma(t, (yr[2] - yr[3]) - f1, f3), fma(t, f1, yr[0]));
         neg = zr < (T)0;
@@ -1181,8 +1161,14 @@ __global__ void quad_kernel(const C2<T>* __restrict__ spec, const T* __restrict_
     }
 }
 
-// Records of a real spectrum (a swept profile's): corner c of cell (k, q) at
-// quads[4 e + c], the moduli being their absolute values.
+// Records of a real spectrum (a swept profile's), cell e = (k, q).  FP32: the
+// 4 corners y_c at quads[4 e + c] (the moduli are their absolute values).
+// FP64 (48 bytes): the coefficients of the bilinear modulus in the
+// reference's algebraic form (interpolate_core :804-812), m0 = |y0|,
+// e1 = |y1| - m0, e3 = |y3| - m0, e2 = (|y2| - |y3|) - e1, so that the
+// visibility pass evaluates A = m0 + t e1 + q (e3 + t e2) with three fused
+// multiply-adds (the same operations on the same values as evaluating it
+// from the corners), then the 4 corners as FP32 for the sign estimate of z.
 template <typename T>
 __global__ void quad_real_kernel(const C2<T>* __restrict__ spec, long long s_row, long long s_col, int C,
                                  const DevState* __restrict__ st, T* __restrict__ quads, long long cap) {
@@ -1200,11 +1186,18 @@ __global__ void quad_real_kernel(const C2<T>* __restrict__ spec, long long s_row
         for (int c = 0; c < 4; ++c) ok = ok && rr[c] < w.W && cc[c] < w.K;
         if (!ok) continue;
         T* rec = quads + e * real_rec<T>();
+        T y[4];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const T y = spec[(long long)rr[c] * s_row + (long long)cc[c] * s_col].x;
-            rec[c] = y;
-            if constexpr (sizeof(T) == 8) reinterpret_cast<float*>(rec + 4)[c] = (float)y;
+        for (int c = 0; c < 4; ++c) y[c] = spec[(long long)rr[c] * s_row + (long long)cc[c] * s_col].x;
+        if constexpr (sizeof(T) == 8) {
+            const T m0 = fabs(y[0]), m1 = fabs(y[1]), m2 = fabs(y[2]), m3 = fabs(y[3]);
+            const T e1 = m1 - m0, e3 = m3 - m0;
+            reinterpret_cast<double2*>(rec)[0] = make_double2(m0, e1);
+            reinterpret_cast<double2*>(rec)[1] = make_double2(e3, (m2 - m3) - e1);
+            *reinterpret_cast<float4*>(rec + 4) = make_float4((float)y[0], (float)y[1], (float)y[2], (float)y[3]);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) rec[c] = y[c];
         }
     }
 }
@@ -1502,7 +1495,7 @@ cudaError_t Launch<T>::rows_profile(const T* intensity, int nr, double Rmin, dou
 template <typename T>
 cudaError_t Launch<T>::cols_profile(const CT* zt, int N, int band0, int band1, const CT* tw, const CT* stw, CT* out,
                                     T* amp_out, long long s_row, long long s_col, const DevState* state, double duv,
-                                    cudaStream_t s, const CT* stw4, T* quads, long long quad_cap) {
+                                    cudaStream_t s, const CT* stw4) {
     if constexpr (sizeof(T) == 8) {  // the FP32 passes keep the paired transforms
     if (stw4 && amp_out && even_dft_ok<T>(N)) {
         FftCfg<T> c;
@@ -1515,8 +1508,7 @@ cudaError_t Launch<T>::cols_profile(const CT* zt, int N, int band0, int band1, c
             auto kern = cols_profile_dct_kernel<T, EE, TT>;
             e = set_smem(kern, sm);
             if (e == cudaSuccess) {
-                kern<<<N / 2 + 1, c.threads, sm, s>>>(zt, N, rmax, tw, stw4, out, amp_out, s_row, s_col, state,
-                                                       quads, quad_cap);
+                kern<<<N / 2 + 1, c.threads, sm, s>>>(zt, N, rmax, tw, stw4, out, amp_out, s_row, s_col, state);
                 e = cudaGetLastError();
             }
         });
