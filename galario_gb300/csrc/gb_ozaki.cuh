@@ -19,24 +19,30 @@
 // K max|a| max|b|.  Every lev_L is a sum of integer products of at most
 // 64 x 64: over one K tile of 64 values, at most 8 x 64 x 4096 = 2^21 in
 // magnitude, so the tensor core's FP32 accumulation adds integers that are
-// all exactly representable and the level sums are exact; the partial sums
-// of the K tiles stay exact in FP32 while (L + 1) K 4096 < 2^24, i.e. for
-// K <= 511.
+// all exactly representable and the level sums of a K tile are exact.
 //
-// ozaki_levels_kernel: C = A B^T in levels, A (M x K) and B (N x K) given as
-// digit planes, K-major bf16 (plane stride a multiple of the row stride).
-// One work item = one 128 x 64 output tile and one K tile of 64: TMA loads
-// the eight A planes (128 x 64) and eight B planes (64 x 64) into shared
-// memory (128-byte swizzle), one thread issues the 36 digit-pair products
-// (4 K steps of tcgen05.mma kind::f16, M = 128, N = 64, K = 16 each) into
-// eight FP32 accumulators in tensor memory (8 x 64 = 512 columns), and four
-// epilogue warps add the eight level tiles of the item into the level buffer
-// P[L][m][n] with vector reductions (red.global.add.v4.f32): the values are
-// integers and every partial and total sum stays below 2^24, so the adds are
-// exact and their order does not matter.  P must be zero before the call;
-// the kernel that reads it clears it.  The grid is persistent (items
-// round-robin over the CTAs): the tile counts come from device-side sizes
-// (the spectrum window).
+// ozaki_levels_kernel: C = A B^T, A (M x K) and B (N x K) given as digit
+// planes, K-major bf16 (plane stride a multiple of the row stride).  One work
+// item = one 128 x 64 output tile and one K tile of 64: TMA loads the eight A
+// planes (128 x 64) and eight B planes (64 x 64) into shared memory (128-byte
+// swizzle), one thread issues the 36 digit-pair products (4 K steps of
+// tcgen05.mma kind::f16, M = 128, N = 64, K = 16 each; fully unrolled, the
+// shared-memory descriptors computed once) into eight FP32 accumulators in
+// tensor memory (8 x 64 = 512 columns).  Four epilogue warps read the eight
+// levels of each element and fold them into two integers,
+//
+//     hi = sum_{L<4} 2^(7 (3 - L)) lev_L,   lo = sum_{4<=L<8} 2^(7 (7 - L)) lev_L,
+//
+// (below 2^43 per K tile), so that sum_L 2^(-7L) lev_L = hi 2^-21 + lo 2^-49,
+// and add them into the output P with 64-bit integer reductions
+// (red.global.add.u64): integer sums, exact and independent of the order of
+// the K tiles, below 2^53 for up to 1023 K tiles (K < 65472), so that they
+// convert to double exactly.  Layout P[(h * N + n) * ldm + m], h = 0 (hi) or
+// 1 (lo), m fastest: the 32 lanes of a warp hold 32 consecutive rows, so
+// every reduction instruction covers 256 contiguous bytes.  Only m < M,
+// n < N are written; P must be zero there on entry, and the kernel that
+// reads P clears it.  The grid is persistent (items round-robin over the
+// CTAs): the tile counts come from device-side sizes (the spectrum window).
 // Every wait is bounded; a wait that runs out sets the error bit, each role
 // stops, the CTA waits (bounded) for what it issued, frees its tensor memory
 // and returns.  Single-GPU code: no multicast.
@@ -55,28 +61,31 @@ constexpr int BM = 128;
 constexpr int BN = 64;
 constexpr int BK = 64;           // bf16 values per K tile: one 128-byte swizzle row
 constexpr int kThreads = 192;    // producer warp, MMA warp, four epilogue warps
-constexpr int kMaxK = 511;       // exact FP32 sums of the K tiles
+constexpr int kMaxK = 1023 * BK; // K tiles whose integer sums stay below 2^53
 constexpr int kABytes = BM * BK * 2;  // one A plane tile
 constexpr int kBBytes = BN * BK * 2;  // one B plane tile
 constexpr int kSmem = 1024 + kPlanes * (kABytes + kBBytes) + 256;
 constexpr int kTmemCols = kLevels * BN;  // 512
 
 // Sizes of one product.  M and N may come from the device (the spectrum
-// window): rows = min(*m_dev, m_max) when m_dev is set; with win_r0/win_W
-// the column count is 1 + the largest |r - N/2| over the window rows.  The
-// level buffer is compact for those sizes: P[(L * Mp + m) * ldp + n] with
-// Mp = M rounded up to 128 and ldp = N rounded up to 4 (Dims below).
+// window): rows = min(*m_dev, m_max) when m_dev is set, columns =
+// min(*n_dev, n_max) when n_dev is set; with win_r0/win_W the rows (win_rows)
+// or the columns number at most 1 + the largest |r - N/2| over the window
+// rows.  The output is compact for those sizes: P[(h * N + n) * ldm + m] with
+// ldm = M rounded up to 32 (Dims below).
 struct Params {
     int m_max, n_max, K;
-    const int* m_dev;            // window K (rows of the first factor), or null
-    const int* win_r0;           // window r0 and W (columns from the window), or null
+    const int* m_dev;            // rows from the device, or null
+    const int* n_dev;            // columns from the device, or null
+    const int* win_r0;           // window r0 and W, or null
     const int* win_W;
+    int win_rows;                // the window bounds the rows (1) or the columns (0)
     int half;                    // N/2 of the image
-    float* P;                    // level buffer (zero on entry)
+    long long* P;                // hi / lo sums (zero on entry where m < M, n < N)
     unsigned* err;
 };
 struct Dims {
-    int M, N, Mp, ldp;
+    int M, N, Mp, ldm;           // Mp: M rounded up to the 128-row tiles
 };
 
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
@@ -96,22 +105,49 @@ __host__ __device__ inline Dims dims_of(int m, int n) {
     d.M = m > 0 ? m : 0;
     d.N = n > 0 ? n : 0;
     d.Mp = (d.M + BM - 1) / BM * BM;
-    d.ldp = (d.N + 3) / 4 * 4;
+    d.ldm = (d.M + 31) / 32 * 32;
     return d;
 }
 __device__ __forceinline__ Dims item_dims(const Params& p) {
     int m = p.m_max, n = p.n_max;
     if (p.m_dev) m = min(m, *((volatile const int*)p.m_dev));
+    if (p.n_dev) n = min(n, *((volatile const int*)p.n_dev));
     if (p.win_r0) {
         const int r0 = *((volatile const int*)p.win_r0), W = *((volatile const int*)p.win_W);
-        n = min(n, max(p.half - r0, r0 + W - 1 - p.half) + 1);
+        const int t1 = max(p.half - r0, r0 + W - 1 - p.half) + 1;
+        if (p.win_rows) m = min(m, t1);
+        else n = min(n, t1);
     }
     return dims_of(m, n);
 }
-__device__ __forceinline__ void red_add_v4(float* dst, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
-    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(__uint_as_float(a)),
-                 "f"(__uint_as_float(b)), "f"(__uint_as_float(c)), "f"(__uint_as_float(d))
+__device__ __forceinline__ void red_add_u64(long long* dst, long long v) {
+    asm volatile("red.global.add.u64 [%0], %1;" ::"l"(dst), "l"(v) : "memory");
+}
+// 8 consecutive accumulator columns of this thread's TMEM lane (values valid after tmem_wait8)
+__device__ __forceinline__ void tmem_ld8_async(uint32_t taddr, uint32_t* r) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+// wait for every outstanding tcgen05.ld of this thread; the 64 registers pass
+// through the wait so that no use is scheduled before it
+__device__ __forceinline__ void tmem_wait64(uint32_t* r) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                   "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
+                   "+r"(r[29]), "+r"(r[30]), "+r"(r[31]), "+r"(r[32]), "+r"(r[33]), "+r"(r[34]), "+r"(r[35]),
+                   "+r"(r[36]), "+r"(r[37]), "+r"(r[38]), "+r"(r[39]), "+r"(r[40]), "+r"(r[41]), "+r"(r[42]),
+                   "+r"(r[43]), "+r"(r[44]), "+r"(r[45]), "+r"(r[46]), "+r"(r[47]), "+r"(r[48]), "+r"(r[49]),
+                   "+r"(r[50]), "+r"(r[51]), "+r"(r[52]), "+r"(r[53]), "+r"(r[54]), "+r"(r[55]), "+r"(r[56]),
+                   "+r"(r[57]), "+r"(r[58]), "+r"(r[59]), "+r"(r[60]), "+r"(r[61]), "+r"(r[62]), "+r"(r[63])
+                 :
                  : "memory");
+}
+// the product sum_L 2^(-7L) lev_L from the two integer sums (one rounding)
+__host__ __device__ inline double combine_hi_lo(long long hi, long long lo) {
+    return fma((double)lo, 0x1p-49, (double)hi * 0x1p-21);
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
@@ -193,8 +229,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            // ---- MMA issuer: planes in arrival order; pair (i, j) once both have landed ----
+            // ---- MMA issuer: planes in arrival order; pair (i, j) once both
+            // have landed.  The order is fixed, so whether a level's
+            // accumulator is fresh is a compile-time fact of the unrolled loops.
             constexpr uint32_t idesc = idesc_bf16(BM, BN);
+            uint64_t da[kPlanes], db[kPlanes];
+#pragma unroll
+            for (int i = 0; i < kPlanes; ++i) {
+                da[i] = sdesc(smem_addr(a_tiles + i * kABytes));
+                db[i] = sdesc(smem_addr(b_tiles + i * kBBytes));
+            }
             int t = 0;
             for (int item = blockIdx.x; item < items && !*abort_flag; item += gridDim.x, ++t) {
                 // the levels of the previous item must have been read out
@@ -202,9 +246,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                     fail();
                     break;
                 }
-                unsigned started = 0u;  // levels whose accumulator has been written
                 bool ok = true;
-                for (int s = 0; s < kPlanes && ok; ++s) {
+                unsigned started = 0u;
+#pragma unroll
+                for (int s = 0; s < kPlanes; ++s) {
+                    if (!ok) break;
                     if (!mbar_wait(&full[s], (uint32_t)(t & 1))) {
                         fail();
                         ok = false;
@@ -212,18 +258,20 @@ __global__ void __launch_bounds__(kThreads, 1)
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     // pairs with max(i, j) = s and i + j <= 7
+#pragma unroll
                     for (int o = 0; o <= s; ++o) {
-                        for (int side = 0; side < (o == s ? 1 : 2); ++side) {
+#pragma unroll
+                        for (int side = 0; side < 2; ++side) {
+                            if (side == 1 && o == s) continue;
                             const int i = side == 0 ? s : o, j = side == 0 ? o : s;
                             const int L = i + j;
                             if (L >= kLevels) continue;
                             const uint32_t acc = tmem + (uint32_t)(L * BN);
-                            const uint32_t ab = smem_addr(a_tiles + i * kABytes), bb = smem_addr(b_tiles + j * kBBytes);
 #pragma unroll
                             for (int kk = 0; kk < BK / 16; ++kk) {
-                                const uint32_t off = kk * 32;  // 16 bf16 = 32 bytes along the swizzled row
+                                // a K step of 16 bf16 = 32 bytes along the swizzled row: +2 in the address field
                                 const uint32_t accumulate = ((started >> L) & 1u) || kk > 0 ? 1u : 0u;
-                                mma_bf16(acc, sdesc(ab + off), sdesc(bb + off), idesc, accumulate);
+                                mma_bf16(acc, da[i] + 2 * kk, db[j] + 2 * kk, idesc, accumulate);
                             }
                             started |= 1u << L;
                         }
@@ -237,7 +285,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (!mbar_wait(done, 0u)) fail();  // every MMA complete before the tensor memory is freed
         }
     } else {
-        // ---- epilogue: lane = tile row; 8 levels x 64 columns per item ----
+        // ---- epilogue: lane = tile row; 8 levels of 8 columns at a time,
+        // folded into the hi / lo integer sums of each element
         const int quarter = warp & 3;
         const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
         int t = 0;
@@ -249,20 +298,29 @@ __global__ void __launch_bounds__(kThreads, 1)
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int row = m0 + quarter * 32 + lane;  // < Mp
+            const int row = m0 + quarter * 32 + lane;
             (void)kt;
-            for (int L = 0; L < kLevels; ++L) {
-                uint32_t x[32], y[32];
-                tmem_ld32_async(tmem + lane_off + (uint32_t)(L * BN), x);
-                tmem_ld32_async(tmem + lane_off + (uint32_t)(L * BN + 32), y);
-                tmem_wait32(x);
-                tmem_wait32(y);
-                float* dst = p.P + ((size_t)L * dm.Mp + row) * dm.ldp + n0;
-                // ldp is a multiple of 4 and n0 of 64: 16-byte reductions inside the row
+            const bool live = row < dm.M;
+            long long* hi_row = p.P + row;
+            long long* lo_row = p.P + (long long)dm.N * dm.ldm + row;
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 8) {
+                uint32_t x[kLevels * 8];
 #pragma unroll
-                for (int c = 0; c < 32; c += 4) {
-                    if (n0 + c < dm.ldp) red_add_v4(dst + c, x[c], x[c + 1], x[c + 2], x[c + 3]);
-                    if (n0 + 32 + c < dm.ldp) red_add_v4(dst + 32 + c, y[c], y[c + 1], y[c + 2], y[c + 3]);
+                for (int L = 0; L < kLevels; ++L) tmem_ld8_async(tmem + lane_off + (uint32_t)(L * BN + c0), x + 8 * L);
+                tmem_wait64(x);
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    const int n = n0 + c0 + c;
+                    long long hi = 0, lo = 0;
+#pragma unroll
+                    for (int L = 0; L < 4; ++L) hi = hi * 128 + (long long)__float2int_rz(__uint_as_float(x[8 * L + c]));
+#pragma unroll
+                    for (int L = 4; L < 8; ++L) lo = lo * 128 + (long long)__float2int_rz(__uint_as_float(x[8 * L + c]));
+                    if (live && n < dm.N) {
+                        red_add_u64(hi_row + (long long)n * dm.ldm, hi);
+                        red_add_u64(lo_row + (long long)n * dm.ldm, lo);
+                    }
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

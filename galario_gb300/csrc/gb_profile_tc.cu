@@ -11,24 +11,28 @@
 //
 // two products with one fixed cosine matrix: D1 = C[0:K] F^T (K x nF), then
 // S' = D1 C[0:T+1]^T (K x (T + 1)), T = max |r - N/2| over the window rows, and
-// window row r takes S'[.][|r - N/2|].  Both products run as FP64-grade
+// window row r takes S'[.][|r - N/2|].  Both run transposed (D1^T = F C^T,
+// S'^T = C D1^T), so that the row of D1 that the next pass splits, and the
+// column of S' that becomes a window column, are contiguous in the products'
+// output (whose fastest index is the row of the first factor).  Both products run as FP64-grade
 // products on the bf16 tensor cores (gb_ozaki.cuh): each operand row as eight
 // balanced base-128 digits relative to the row's exponent, the 36 digit-pair
-// products with i + j <= 7 summed exactly in integer levels.
+// products with i + j <= 7 summed exactly in integer levels and folded into
+// two exact 64-bit integer sums per element.
 //
 // Passes (one stream, no host round trip; K, r0, W come from the device
 // window written by the extent pass):
 //   oz_fold_kernel       the quadrant of the sweep (reference sweep_core
 //                        :1048-1071, central pixel :1136-1153), one row per
 //                        block, its row exponent and digits
-//   ozaki_levels_kernel  levels of D1 = C[0:K] F^T
-//   oz_mid_kernel        D1 from its levels (which it clears), one row per
+//   ozaki_levels_kernel  D1^T = F C[0:K]^T as integer sums
+//   oz_mid_kernel        D1 from its sums (which it clears), one row per
 //                        block, its row exponent and digits
-//   ozaki_levels_kernel  levels of S' = D1 C[0:T+1]^T
-//   oz_out_kernel        S' from its levels (which it clears) -> window rows
+//   ozaki_levels_kernel  S'^T = C[0:T+1] D1^T as integer sums
+//   oz_out_kernel        S' from its sums (which it clears) -> window rows
 //                        N/2 - t and N/2 + t and their moduli (the cell
 //                        records are built from the window afterwards)
-// The level buffers are zero between calls: allocated zeroed, and every entry
+// The sum buffers are zero between calls: allocated zeroed, and every entry
 // the level kernel adds to is read and cleared by the pass after it.
 #include <cuda_runtime.h>
 #include <math.h>
@@ -46,21 +50,24 @@ namespace gbg {
 
 namespace {
 
-constexpr int kFoldThreads = 128;
-constexpr int kPerThread = 4;                 // kFoldThreads * kPerThread > oz::kMaxK
+constexpr int kFoldThreads = 256;
+constexpr int kPerThread = 8;                 // values of a row per thread: rows of up to 2048
+constexpr int kMaxRow = kFoldThreads * kPerThread;
 constexpr int kBadRow = -0x7fffffff;          // row exponent of a row with a NaN or infinite value
 
-__device__ __forceinline__ double block_max128(double v, double* red) {
+__device__ __forceinline__ double block_max(double v, double* red) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
-    const double m = fmax(fmax(red[0], red[1]), fmax(red[2], red[3]));
+    double m = red[0];
+#pragma unroll
+    for (int w = 1; w < kFoldThreads / 32; ++w) m = fmax(m, red[w]);
     __syncthreads();
     return m;
 }
 
-// digits of a row: v[i] at column threadIdx.x + 128 i (< n), relative to exponent e
+// digits of a row: v[i] at column threadIdx.x + kFoldThreads i (< n), relative to exponent e
 __device__ __forceinline__ void write_digits(const double* v, int n, int e, unsigned short* __restrict__ dst,
                                              long long plane) {
 #pragma unroll
@@ -74,24 +81,13 @@ __device__ __forceinline__ void write_digits(const double* v, int n, int e, unsi
     }
 }
 
-// sum_L 2^(-7 L) P[L] at one (row, column) of a compact level buffer, clearing
-// it.  The levels are integers below 2^24 in magnitude (held exactly in
-// FP32), so the sum is formed in integer arithmetic, hi = levels 0-3 and
-// lo = levels 4-7 as base-128 numbers (below 2^46 each), and rounded once:
-// hi 2^-21 + lo 2^-49 in one fused multiply-add (no FP64 conversions of the
-// eight levels, which run on the FP64 pipe).
-__device__ __forceinline__ double take_levels(float* __restrict__ P, long long level_stride) {
-    float f[oz::kLevels];
-#pragma unroll
-    for (int L = 0; L < oz::kLevels; ++L) f[L] = P[(long long)L * level_stride];
-#pragma unroll
-    for (int L = 0; L < oz::kLevels; ++L) P[(long long)L * level_stride] = 0.f;
-    long long hi = 0, lo = 0;
-#pragma unroll
-    for (int L = 0; L < 4; ++L) hi = hi * 128 + (long long)__float2int_rz(f[L]);
-#pragma unroll
-    for (int L = 4; L < 8; ++L) lo = lo * 128 + (long long)__float2int_rz(f[L]);
-    return fma((double)lo, 0x1p-49, (double)hi * 0x1p-21);
+// sum_L 2^(-7 L) lev_L of one product element from its hi / lo integer sums
+// (see ozaki_levels_kernel), clearing them for the next call
+__device__ __forceinline__ double take_sum(long long* __restrict__ hi, long long lo_off) {
+    const long long h = hi[0], l = hi[lo_off];
+    hi[0] = 0;
+    hi[lo_off] = 0;
+    return oz::combine_hi_lo(h, l);
 }
 
 // x 2^n from exponent-field arithmetic (exact while the result is a normal number)
@@ -110,7 +106,7 @@ __global__ void __launch_bounds__(kFoldThreads) oz_fold_kernel(const double* __r
                                                                double inv_cos_inc, int rmax, double central, int N,
                                                                int nF, int ldF, unsigned short* __restrict__ fd,
                                                                int* __restrict__ ef) {
-    __shared__ double red[4];
+    __shared__ double red[kFoldThreads / 32];
     const int a = blockIdx.x;
     const int n = N / 2, off = N / 2 - rmax;
     const double sr_to_px = dxy * dxy;
@@ -128,64 +124,62 @@ __global__ void __launch_bounds__(kFoldThreads) oz_fold_kernel(const double* __r
             mx = (m > mx || m != m) ? m : mx;  // NaN propagates
         }
     }
-    mx = block_max128(isfinite(mx) ? mx : INFINITY, red);
+    mx = block_max(isfinite(mx) ? mx : INFINITY, red);
     const bool bad = !isfinite(mx);
     const int e = bad ? kBadRow : oz::row_exponent(mx);
     if (threadIdx.x == 0) ef[a] = e;
     if (!bad) write_digits(v, nF, e, fd + (long long)a * ldF, (long long)nF * ldF);
 }
 
-// Rows k of D1 = C[0:K] F^T from its levels (rows [K, Mp) only cleared), as
-// digits of a row-major K x nF operand (plane stride planeD, row stride ldF).
+// Rows k of D1 from the sums of D1^T (which it clears; D1[k][a] at column k,
+// row a, so a row of D1 is contiguous), as digits of a row-major K x nF
+// operand (plane stride planeD, row stride ldF).
 __global__ void __launch_bounds__(kFoldThreads) oz_mid_kernel(oz::Params p, const int* __restrict__ ec,
                                                               const int* __restrict__ ef, int nF, int ldF,
                                                               long long planeD, unsigned short* __restrict__ dd,
                                                               int* __restrict__ ed) {
-    __shared__ double red[4];
-    const oz::Dims dm = oz::item_dims(p);  // the level pass's sizes
-    const long long ls = (long long)dm.Mp * dm.ldp;
-    for (int k = blockIdx.x; k < dm.Mp; k += gridDim.x) {
-        const bool live = k < dm.M;
-        const int eck = live ? ec[k] : 0;
+    __shared__ double red[kFoldThreads / 32];
+    const oz::Dims dm = oz::item_dims(p);  // M = nF rows (a), N = K columns (k)
+    const long long lo_off = (long long)dm.N * dm.ldm;
+    for (int k = blockIdx.x; k < dm.N; k += gridDim.x) {
+        const int eck = ec[k];
         double v[kPerThread];
         double mx = 0.0;
 #pragma unroll
         for (int i = 0; i < kPerThread; ++i) {
             const int a = threadIdx.x + kFoldThreads * i;
             v[i] = 0.0;
-            if (a < dm.ldp) {
-                const double acc = take_levels(p.P + (long long)k * dm.ldp + a, ls);
-                if (live && a < nF) {
-                    const int ea = ef[a];
-                    v[i] = (ea == kBadRow || eck == kBadRow) ? (double)NAN : scale2(acc, eck + ea - 12);
-                    const double m = fabs(v[i]);
-                    mx = (m > mx || m != m) ? m : mx;
-                }
+            if (a < nF) {
+                const double acc = take_sum(p.P + (long long)k * dm.ldm + a, lo_off);
+                const int ea = ef[a];
+                v[i] = (ea == kBadRow || eck == kBadRow) ? (double)NAN : scale2(acc, eck + ea - 12);
+                const double m = fabs(v[i]);
+                mx = (m > mx || m != m) ? m : mx;
             }
         }
-        mx = block_max128(isfinite(mx) ? mx : INFINITY, red);
-        if (live) {
-            const bool bad = !isfinite(mx);
-            const int e = bad ? kBadRow : oz::row_exponent(mx);
-            if (threadIdx.x == 0) ed[k] = e;
-            if (!bad) write_digits(v, nF, e, dd + (long long)k * ldF, planeD);
-        }
+        mx = block_max(isfinite(mx) ? mx : INFINITY, red);
+        const bool bad = !isfinite(mx);
+        const int e = bad ? kBadRow : oz::row_exponent(mx);
+        if (threadIdx.x == 0) ed[k] = e;
+        if (!bad) write_digits(v, nF, e, dd + (long long)k * ldF, planeD);
     }
 }
 
-// S'[k][t] from its levels (the whole compact region cleared), written to
-// window rows N/2 -+ t of column k: the spectrum value and its modulus.
+// S'[k][t] from the sums of S'^T (which it clears; consecutive threads take
+// consecutive t), written to window rows N/2 -+ t of column k: the spectrum
+// value and its modulus.
 __global__ void __launch_bounds__(256) oz_out_kernel(oz::Params p, const int* __restrict__ ed,
                                                      const int* __restrict__ ec, int N,
                                                      const DevState* __restrict__ st, C2<double>* __restrict__ out,
                                                      double* __restrict__ amp, long long s_row, long long s_col) {
-    const oz::Dims dm = oz::item_dims(p);
+    const oz::Dims dm = oz::item_dims(p);  // M = T + 1 rows (t), N = K columns (k)
     const Window w = get_window(-1, -1, -1, st);
-    const long long ls = (long long)dm.Mp * dm.ldp;
-    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < ls; e += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(e / dm.ldp), t = (int)(e - (long long)k * dm.ldp);
-        const double acc = take_levels(p.P + e, ls);
-        if (k >= dm.M || t >= dm.N) continue;
+    const long long lo_off = (long long)dm.N * dm.ldm;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < lo_off;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e / dm.ldm), t = (int)(e - (long long)k * dm.ldm);
+        if (t >= dm.M) continue;
+        const double acc = take_sum(p.P + e, lo_off);
         const int ek = ed[k];
         const double f = ek == kBadRow ? (double)NAN : scale2(acc, ek + ec[t] - 12);
 #pragma unroll
@@ -234,7 +228,7 @@ inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
 struct ProfileTc {
     int N = 0, nF = 0, ldF = 0;  // geometry of the cosine digits and of the operands
     Buf cd, ec, fd, ef, dd, ed, p1, p2;
-    CUtensorMap map_ca{}, map_cb{}, map_f{}, map_d{};
+    CUtensorMap map_ca{}, map_cb{}, map_f{}, map_d{};  // C as A / B, F as A, D1 as B
     bool maps = false;
     bool smem_attr = false;  // the level kernel's shared-memory limit raised (per device, as this state)
 };
@@ -256,7 +250,7 @@ bool profile_tc_ok(int N, int rmax) {
     const char* v = std::getenv("GALARIO_TC");
     if (v && v[0] == '0') return false;
     const int nF = profile_tc_quadrant(N, rmax);
-    return N >= 16 && N % 2 == 0 && N <= 16384 && nF >= 1 && nF <= oz::kMaxK && tc::encode_fn() != nullptr;
+    return N >= 16 && N % 2 == 0 && N <= 16384 && nF >= 1 && nF <= kMaxRow && tc::encode_fn() != nullptr;
 }
 
 // the digits of C[j][c] = w_c cos(2 pi c j / N), j <= N/2, c < nF (cosines
@@ -310,21 +304,21 @@ static cudaError_t prepare(ProfileTc* t, int N, int nF) {
         moved = true;
     }
     const long long planeF = (long long)nF * ldF, planeD = (long long)C * ldF;
-    const int Mp = round_up(C, oz::BM);
+    const int ldmF = round_up(nF, 32), ldmC = round_up(C, 32);  // rows of the products' sums
     e = t->fd.get(sizeof(unsigned short) * oz::kPlanes * planeF, false, &fresh);
     moved |= fresh;
     if (e == cudaSuccess) e = t->ef.get(sizeof(int) * nF, false, &fresh);
     if (e == cudaSuccess) e = t->dd.get(sizeof(unsigned short) * oz::kPlanes * planeD, true, &fresh);
     moved |= fresh;
     if (e == cudaSuccess) e = t->ed.get(sizeof(int) * C, false, &fresh);
-    if (e == cudaSuccess) e = t->p1.get(sizeof(float) * oz::kLevels * (size_t)Mp * round_up(nF, 4), true, &fresh);
-    if (e == cudaSuccess) e = t->p2.get(sizeof(float) * oz::kLevels * (size_t)Mp * round_up(C, 4), true, &fresh);
+    if (e == cudaSuccess) e = t->p1.get(sizeof(long long) * 2 * (size_t)ldmF * C, true, &fresh);
+    if (e == cudaSuccess) e = t->p2.get(sizeof(long long) * 2 * (size_t)ldmC * C, true, &fresh);
     if (e != cudaSuccess) return e;
     if (moved || !t->maps) {
         t->maps = oz::make_map(&t->map_ca, t->cd.p, nF, C, ldF, planeD, oz::BM) &&
                   oz::make_map(&t->map_cb, t->cd.p, nF, C, ldF, planeD, oz::BN) &&
-                  oz::make_map(&t->map_f, t->fd.p, nF, nF, ldF, planeF, oz::BN) &&
-                  oz::make_map(&t->map_d, t->dd.p, nF, C, ldF, planeD, oz::BM);
+                  oz::make_map(&t->map_f, t->fd.p, nF, nF, ldF, planeF, oz::BM) &&
+                  oz::make_map(&t->map_d, t->dd.p, nF, C, ldF, planeD, oz::BN);
         if (!t->maps) return cudaErrorInvalidValue;
     }
     return cudaSuccess;
@@ -352,15 +346,16 @@ cudaError_t profile_tc_window(ProfileTc* t, int N, DevState* st, C2<double>* out
         t->smem_attr = true;
     }
     const int grid = num_sms();
+    // D1^T = F C[0:K]^T: rows a < nF, columns k < K (the window)
     oz::Params p1{};
-    p1.m_max = C;
-    p1.n_max = nF;
+    p1.m_max = nF;
+    p1.n_max = C;
     p1.K = nF;
-    p1.m_dev = &st->win_K;
+    p1.n_dev = &st->win_K;
     p1.half = N / 2;
-    p1.P = static_cast<float*>(t->p1.p);
+    p1.P = static_cast<long long*>(t->p1.p);
     p1.err = &st->err;
-    oz::ozaki_levels_kernel<<<grid, oz::kThreads, oz::kSmem, s>>>(t->map_ca, t->map_f, p1);
+    oz::ozaki_levels_kernel<<<grid, oz::kThreads, oz::kSmem, s>>>(t->map_f, t->map_cb, p1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     oz_mid_kernel<<<2 * grid, kFoldThreads, 0, s>>>(p1, static_cast<const int*>(t->ec.p),
@@ -368,12 +363,19 @@ cudaError_t profile_tc_window(ProfileTc* t, int N, DevState* st, C2<double>* out
                                                      static_cast<unsigned short*>(t->dd.p), static_cast<int*>(t->ed.p));
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    oz::Params p2 = p1;
+    // S'^T = C[0:T+1] D1^T: rows t <= T (the window rows' distances), columns k < K
+    oz::Params p2{};
+    p2.m_max = C;
     p2.n_max = C;
+    p2.K = nF;
+    p2.n_dev = &st->win_K;
     p2.win_r0 = &st->win_r0;
     p2.win_W = &st->win_W;
-    p2.P = static_cast<float*>(t->p2.p);
-    oz::ozaki_levels_kernel<<<grid, oz::kThreads, oz::kSmem, s>>>(t->map_d, t->map_cb, p2);
+    p2.win_rows = 1;
+    p2.half = N / 2;
+    p2.P = static_cast<long long*>(t->p2.p);
+    p2.err = &st->err;
+    oz::ozaki_levels_kernel<<<grid, oz::kThreads, oz::kSmem, s>>>(t->map_ca, t->map_d, p2);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     oz_out_kernel<<<2 * grid, 256, 0, s>>>(p2, static_cast<const int*>(t->ed.p), static_cast<const int*>(t->ec.p), N,

@@ -1,12 +1,14 @@
-// Unit test of the bf16 tensor-core level products (galario_gb300/csrc/gb_ozaki.cuh).
+// Unit test of the bf16 tensor-core digit products (galario_gb300/csrc/gb_ozaki.cuh).
 //
 // 1. Exactness: random integer digit planes (|d| <= 64) for A (M x K) and
-//    B (N x K); every level sum lev_L[m][n] = sum_{i+j=L} sum_k A_i B_j must
-//    equal the int64 result exactly, including M, N, K that are not multiples
-//    of the tiles (zero fill) and K up to the 511 bound with every digit at
-//    +-64 (the largest sums).
+//    B (N x K); the kernel's two integer sums per element,
+//    hi = sum_{L<4} 2^(7(3-L)) lev_L and lo = sum_{4<=L<8} 2^(7(7-L)) lev_L
+//    with lev_L = sum_{i+j=L} sum_k A_i B_j, must equal the int64 result
+//    exactly, including M, N, K that are not multiples of the tiles (zero
+//    fill), every digit at +-64 (the largest level sums of a K tile) and K of
+//    many tiles.
 // 2. FP64 products: random doubles with rows of widely different scales, the
-//    digits of digits8, the level kernel, and the level combination in double;
+//    digits of digits8, the kernel, and the sums combined in double;
 //    compared with a long double product, the error must stay below
 //    2^-50 K max|a_row| max|b_row| for every element.
 // Prints one line per case and exits nonzero on the first failure.
@@ -55,8 +57,8 @@ struct Planes {
     }
 };
 
-// level sums on the GPU: P[L][m][n] (compact, Mp x ldp)
-static std::vector<float> run_levels(const Planes& A, const Planes& B, oz::Dims* dims) {
+// the kernel's sums on the GPU: P[(h * N + n) * ldm + m], h = 0 (hi), 1 (lo)
+static std::vector<long long> run_levels(const Planes& A, const Planes& B, oz::Dims* dims) {
     CUtensorMap am, bm;
     if (!oz::make_map(&am, A.d, A.K, A.rows, A.ld, (long long)A.rows * A.ld, oz::BM) ||
         !oz::make_map(&bm, B.d, B.K, B.rows, B.ld, (long long)B.rows * B.ld, oz::BN)) {
@@ -64,11 +66,11 @@ static std::vector<float> run_levels(const Planes& A, const Planes& B, oz::Dims*
         std::exit(2);
     }
     const oz::Dims dm = oz::dims_of(A.rows, B.rows);
-    float* P = nullptr;
+    long long* P = nullptr;
     unsigned* err = nullptr;
-    const size_t np = (size_t)oz::kLevels * dm.Mp * dm.ldp;
-    CK(cudaMalloc(&P, np * 4));
-    CK(cudaMemset(P, 0, np * 4));
+    const size_t np = (size_t)2 * dm.N * dm.ldm;
+    CK(cudaMalloc(&P, np * 8));
+    CK(cudaMemset(P, 0, np * 8));
     CK(cudaMalloc(&err, 4));
     CK(cudaMemset(err, 0, 4));
     oz::Params p{};
@@ -89,8 +91,8 @@ static std::vector<float> run_levels(const Planes& A, const Planes& B, oz::Dims*
         std::printf("kernel reported error %u\n", herr);
         std::exit(1);
     }
-    std::vector<float> out(np);
-    CK(cudaMemcpy(out.data(), P, np * 4, cudaMemcpyDeviceToHost));
+    std::vector<long long> out(np);
+    CK(cudaMemcpy(out.data(), P, np * 8, cudaMemcpyDeviceToHost));
     cudaFree(P);
     cudaFree(err);
     *dims = dm;
@@ -110,24 +112,27 @@ static int exact_case(int M, int N, int K, bool extreme, unsigned seed) {
     A.upload();
     B.upload();
     oz::Dims dm;
-    const std::vector<float> P = run_levels(A, B, &dm);
+    const std::vector<long long> P = run_levels(A, B, &dm);
     long long bad = 0, maxabs = 0;
-    for (int L = 0; L < oz::kLevels; ++L)
-        for (int m = 0; m < M; ++m)
-            for (int n = 0; n < N; ++n) {
-                long long ref = 0;
+    for (int m = 0; m < M; ++m)
+        for (int n = 0; n < N; ++n) {
+            long long lev[oz::kLevels] = {0};
+            for (int L = 0; L < oz::kLevels; ++L)
                 for (int i = 0; i <= L; ++i) {
                     const int j = L - i;
                     if (i >= oz::kPlanes || j >= oz::kPlanes) continue;
-                    for (int k = 0; k < K; ++k) ref += (long long)A.v[A.at(i, m, k)] * B.v[B.at(j, n, k)];
+                    for (int k = 0; k < K; ++k) lev[L] += (long long)A.v[A.at(i, m, k)] * B.v[B.at(j, n, k)];
                 }
-                maxabs = std::max(maxabs, std::llabs(ref));
-                const float got = P[((size_t)L * dm.Mp + m) * dm.ldp + n];
-                if ((double)got != (double)ref) {
-                    if (bad < 5) std::printf("  level %d (%d, %d): got %.1f want %lld\n", L, m, n, got, ref);
-                    ++bad;
-                }
+            long long hi = 0, lo = 0;
+            for (int L = 0; L < 4; ++L) hi = hi * 128 + lev[L];
+            for (int L = 4; L < 8; ++L) lo = lo * 128 + lev[L];
+            for (int L = 0; L < oz::kLevels; ++L) maxabs = std::max(maxabs, std::llabs(lev[L]));
+            const long long ghi = P[(size_t)n * dm.ldm + m], glo = P[((size_t)dm.N + n) * dm.ldm + m];
+            if (ghi != hi || glo != lo) {
+                if (bad < 5) std::printf("  (%d, %d): got (%lld, %lld) want (%lld, %lld)\n", m, n, ghi, glo, hi, lo);
+                ++bad;
             }
+        }
     std::printf("exact M=%d N=%d K=%d%s: %lld mismatches, max |level| %lld (2^%.1f)\n", M, N, K,
                 extreme ? " (every digit 64)" : "", bad, maxabs, std::log2((double)maxabs));
     return bad == 0 ? 0 : 1;
@@ -165,12 +170,11 @@ static int fp64_case(int M, int N, int K, unsigned seed) {
     A.upload();
     B.upload();
     oz::Dims dm;
-    const std::vector<float> P = run_levels(A, B, &dm);
+    const std::vector<long long> P = run_levels(A, B, &dm);
     double worst = 0;
     for (int m = 0; m < M; ++m)
         for (int n = 0; n < N; ++n) {
-            double acc = 0;
-            for (int L = oz::kLevels - 1; L >= 0; --L) acc = std::fma(acc, 0x1p-7, (double)P[((size_t)L * dm.Mp + m) * dm.ldp + n]);
+            const double acc = oz::combine_hi_lo(P[(size_t)n * dm.ldm + m], P[((size_t)dm.N + n) * dm.ldm + m]);
             const double got = std::ldexp(acc, ea[m] + eb[n] - 12);
             long double ref = 0, amax = 0, bmax = 0;
             for (int k = 0; k < K; ++k) {
@@ -191,10 +195,12 @@ int main() {
     int fails = 0;
     fails += exact_case(128, 64, 64, false, 1);
     fails += exact_case(240, 130, 343, false, 2);   // ragged sizes of the nxy=4096 profile products
-    fails += exact_case(200, 130, 511, true, 3);    // the largest level sums
+    fails += exact_case(200, 130, 511, true, 3);    // the largest level sums of every K tile
     fails += exact_case(37, 5, 9, false, 4);        // one partial tile
+    fails += exact_case(130, 70, 2000, true, 7);    // many K tiles (32), every digit 64
     fails += fp64_case(240, 242, 343, 5);
     fails += fp64_case(130, 70, 100, 6);
+    fails += fp64_case(150, 200, 1500, 8);
     std::printf(fails ? "FAILED %d\n" : "OK\n", fails);
     return fails ? 1 : 0;
 }

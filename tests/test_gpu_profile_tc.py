@@ -2,11 +2,11 @@
 
 The FP64 chi2Profile / sampleProfile compute the spectrum window as two
 cosine-matrix products on the bf16 tensor cores (eight-digit split, exact
-integer levels) whenever the quadrant of the sweep has at most 511 columns;
+integer sums) whenever the quadrant of the sweep has at most 2048 columns;
 GALARIO_TC=0 keeps the row and column transforms.  Both must agree with the
 oracle within the double tolerances, and with each other to rounding level,
 on the benchmarked workload and on geometries that reach the edges of the
-path: a quadrant at the 511 limit and one beyond it (which falls back), a
+path: quadrants of several K tiles and one beyond 2048 (which falls back), a
 profile wider than the image (rmax clamped to nxy/2, the edge row and column
 carry emission), even sizes that are not powers of two, and a window that
 covers every column (the flat-index wrap of the last column).
@@ -67,8 +67,9 @@ def test_bench_workload_tc_vs_transforms(monkeypatch, oracle_port):
     (250, 500, 10 * deg, 0.45),    # the same at an even size that is not a power of two
     (1000, 586, 60 * deg, 0.49),   # non power of two, nF = 501, window near the full half-plane
     (1536, 450, 20 * deg, 0.3),
-    (2048, 511, 40 * deg, 0.3),    # quadrant of exactly 511 columns (the exact-level limit)
-    (2048, 600, 40 * deg, 0.3),    # quadrant beyond 511: the transforms run
+    (2048, 511, 40 * deg, 0.3),    # quadrant of 511 columns: 8 K tiles, the last one partial
+    (2048, 600, 40 * deg, 0.3),    # 10 K tiles
+    (8192, 2100, 30 * deg, 0.05),  # quadrant beyond 2048 columns: the transforms run
 ])
 def test_geometries_against_oracle(monkeypatch, oracle_port, nxy, rmax_target, inc, reach):
     import galario_gb300 as g
