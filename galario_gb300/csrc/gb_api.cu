@@ -127,6 +127,9 @@ struct Ctx {
     // tail overlaps the next chunk's start
     cudaStream_t vis2 = nullptr;
     cudaEvent_t ev_win = nullptr, ev_vis2 = nullptr;
+    // device-resident FP64 profiles: the extent pass runs on `side` beside
+    // the sweep's fold (which does not need the window)
+    cudaEvent_t ev_ext_start = nullptr, ev_ext_done = nullptr;
     DevBuf state, partials, img, prof, u, v, re, im, w, vis, zt, win, amp, quad, urot, vrot;
     double2* phase_tab = nullptr;  // table of the FP64 phase shift (PHASE_T entries)
     ProfileTc* ptc = nullptr;      // tensor-core spectrum of FP64 profiles (created on first use)
@@ -169,6 +172,8 @@ struct Ctx {
         CK(cudaStreamCreateWithFlags(&vis2, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&ev_win, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&ev_vis2, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ev_ext_start, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&ev_ext_done, cudaEventDisableTiming));
         for (auto& e : ev_chunk) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         CK(cudaMallocHost(&host_state, sizeof(DevState)));
         int pageable = 0;
@@ -449,16 +454,25 @@ template <typename T> struct Pipe {
         size_t nparts = 0;
         for (const auto& r : ranges) nparts += (size_t)L::vis_grid(std::max(1, r.second - r.first));
         double* partials = as<double>(c.partials, nparts);
-        if (!have_extent && !ov) timed(c, s, ST_EXTENT, [&] { CK(L::extent(u, v, nd, N, duv, st, s)); });
+        // FP64 swept profiles whose quadrant fits the tensor-core products:
+        // the window as two cosine-matrix products (gb_profile_tc.cu) instead
+        // of the row and column transforms
+        const bool tc_prof = !img && sizeof(T) == 8 && profile_tc_ok(N, pg->rmax);
+        // the extent pass beside the tensor-core path's fold, on the side stream
+        const bool ext_side = tc_prof && !have_extent && !ov;
+        if (ext_side) {
+            CK(cudaEventRecord(c.ev_ext_start, s));
+            CK(cudaStreamWaitEvent(c.side, c.ev_ext_start, 0));
+            timed(c, c.side, ST_EXTENT, [&] { CK(L::extent(u, v, nd, N, duv, st, c.side)); });
+            CK(cudaEventRecord(c.ev_ext_done, c.side));
+        } else if (!have_extent && !ov) {
+            timed(c, s, ST_EXTENT, [&] { CK(L::extent(u, v, nd, N, duv, st, s)); });
+        }
         int band0 = 0, band1 = N;
         const CT* stw_rows = c.stage_tw<T>(N / 2 > 0 ? N / 2 : 1);
         const CT* stw_cols = c.stage_tw<T>(N);
         // FP64 swept profiles: rows and columns as even-sequence transforms (FFT
         // length N/4); the FP32 passes are faster as paired transforms
-        // FP64 swept profiles whose quadrant fits the exact level sums: the
-        // window as two cosine-matrix products on the tensor cores
-        // (gb_profile_tc.cu) instead of the row and column transforms
-        const bool tc_prof = !img && sizeof(T) == 8 && profile_tc_ok(N, pg->rmax);
         const CT* stw_q = (!img && !tc_prof && sizeof(T) == 8 && even_dft_ok<T>(N))
                               ? c.stage_tw<T>(N / 4, even_dft_e<T>(N))
                               : nullptr;
@@ -483,6 +497,7 @@ template <typename T> struct Pipe {
             CK(cudaStreamWaitEvent(s, ov->ev_uv, 0));
             if (!ov->extent_done) timed(c, s, ST_EXTENT, [&] { CK(L::extent(u, v, nd, N, duv, st, s)); });
         }
+        if (ext_side) CK(cudaStreamWaitEvent(s, c.ev_ext_done, 0));
         // window layout: column k at win + k*N, rows [r0, r0+W) contiguous
         timed(c, s, ST_COLS, [&] {
             if (img) {

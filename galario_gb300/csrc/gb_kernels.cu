@@ -1321,7 +1321,12 @@ cudaError_t Launch<T>::extent(const T* u, const T* v, int nd, int N, double duv,
                               T* u_out, T* v_out) {
     if ((u_out == nullptr) != (v_out == nullptr)) return cudaErrorInvalidValue;
     const int threads = u_out ? 128 : 256;
-    int blocks = (nd + threads - 1) / threads;
+    // device arrays: as many threads as give each one iteration of the
+    // four-vector loop (eight 16-byte loads in flight per thread); the
+    // earlier grid of 8 CTAs per SM left most threads loading one vector at a
+    // time in the tail loop
+    const int per_thread = u_out ? 1 : 4 * (16 / (int)sizeof(T));
+    int blocks = (int)(((long long)nd + (long long)threads * per_thread - 1) / ((long long)threads * per_thread));
     // staging from host memory: one CTA per SM keeps enough loads in flight
     // to fill the host link and leaves the SMs to the row pass beside it
     const int cap = num_sms() * (u_out ? 1 : 8);

@@ -73,12 +73,42 @@ def test_sample_image_double(g, orc, pars, origin):
     assert rel_max(vg, vo) <= DP_V
 
 
-@pytest.mark.parametrize("nxy,nd", [(64, 500), (1024, 100000)])
-def test_chi2_image_double_config0(g, orc, nxy, nd):
+def test_chi2_image_double_config0(g, orc):
+    """The reference's CPU-runnable configuration: chi2Image in float64,
+    nxy = 1024, dxy = 0.01 arcsec, a Gaussian ring (r0 = 0.3", sigma = 0.05")
+    of 0.1 Jy, 1e5 uv points with radius log-uniform in [1e4, 2e6] wavelengths
+    and uniform angle, observations = the reference's sampleImage plus
+    Gaussian noise with sigma uniform in [0.5, 1.5] mJy and w = 1/sigma^2,
+    dRA = 0.05", dDec = -0.03", origin 'upper', seed 0."""
+    nxy, dxy, nd = 1024, 0.01 * arcsec, 100000
+    img = _ring_image(nxy, dxy)
+    u, v = uv_log_uniform(nd, 1e4, 2e6, seed=0)
+    kw = dict(dRA=0.05 * arcsec, dDec=-0.03 * arcsec, PA=0., origin='upper')
+    model = orc["double"].sampleImage(img, dxy, u, v, **kw)
+    vg = g.double.sampleImage(img, dxy, u, v, **kw)
+    assert rel_max(vg, model) <= DP_V
+    rng = np.random.default_rng(0)
+    sigma = rng.uniform(0.5e-3, 1.5e-3, nd)
+    n_re, n_im = rng.normal(0, sigma), rng.normal(0, sigma)
+    re, im, w = model.real + n_re, model.imag + n_im, 1. / sigma ** 2
+    cg = g.double.chi2Image(img, dxy, u, v, re, im, w, **kw)
+    co = orc["double"].chi2Image(img, dxy, u, v, re, im, w, **kw)
+    assert abs(cg - co) / abs(co) <= DP_CHI2
+    # the exact model leaves the noise
+    noise = np.sum(w * (n_re ** 2 + n_im ** 2))
+    assert abs(cg - noise) / noise <= 1e-9
+    # a model shifted by 0.01" is worse than the true one
+    kw2 = dict(kw, dRA=0.06 * arcsec)
+    assert g.double.chi2Image(img, dxy, u, v, re, im, w, **kw2) > cg
+
+
+def test_chi2_image_double_small(g, orc):
+    """A small image with uv points up to 0.49 of the spectrum half-width."""
+    nxy, nd = 64, 500
     dxy = 0.01 * arcsec * 1024 / nxy
     img = _ring_image(nxy, dxy)
     duv = 1 / (nxy * dxy)
-    u, v = uv_log_uniform(nd, 1e4 * (64 / nxy if nxy < 1024 else 1), 0.49 * nxy / 2 * duv, seed=0)
+    u, v = uv_log_uniform(nd, 1e4 * 64 / nxy, 0.49 * nxy / 2 * duv, seed=0)
     re, im, w = _obs(nd)
     kw = dict(dRA=0.05 * arcsec, dDec=-0.03 * arcsec, PA=0.)
     cg = g.double.chi2Image(img, dxy, u, v, re, im, w, **kw)
