@@ -28,21 +28,22 @@
 // swizzle), one thread issues the 36 digit-pair products (4 K steps of
 // tcgen05.mma kind::f16, M = 128, N = 64, K = 16 each; fully unrolled, the
 // shared-memory descriptors computed once) into eight FP32 accumulators in
-// tensor memory (8 x 64 = 512 columns).  Four epilogue warps read the eight
-// levels of each element and fold them into two integers,
+// tensor memory (8 x 64 = 512 columns).  Eight epilogue warps (two per lane
+// quarter, 32 columns each) read the eight levels of each element and fold
+// them into one integer in units of 2^-35,
 //
-//     hi = sum_{L<4} 2^(7 (3 - L)) lev_L,   lo = sum_{4<=L<8} 2^(7 (7 - L)) lev_L,
+//     V = sum_{L<=5} 2^(7 (5 - L)) lev_L + round((2^7 lev_6 + lev_7) / 2^14),
 //
-// (below 2^43 per K tile), so that sum_L 2^(-7L) lev_L = hi 2^-21 + lo 2^-49,
-// and add them into the output P with 64-bit integer reductions
-// (red.global.add.u64): integer sums, exact and independent of the order of
-// the K tiles, below 2^53 for up to 1023 K tiles (K < 65472), so that they
-// convert to double exactly.  Layout P[(h * N + n) * ldm + m], h = 0 (hi) or
-// 1 (lo), m fastest: the 32 lanes of a warp hold 32 consecutive rows, so
-// every reduction instruction covers 256 contiguous bytes.  Only m < M,
-// n < N are written; P must be zero there on entry, and the kernel that
-// reads P clears it.  The grid is persistent (items round-robin over the
-// CTAs): the tile counts come from device-side sizes (the spectrum window).
+// (the last two levels rounded to that unit, half up: at most 2^-36 of
+// 2^(7*5) per K tile, below 2^-52 of K max|a| max|b| in the product) and add
+// it into the output P with a 64-bit integer reduction (red.global.add.u64):
+// integer sums, exact and independent of the order of the K tiles, below
+// 2^62 for up to 32 K tiles.  Layout P[n * ldm + m], m fastest: the 32 lanes
+// of a warp hold 32 consecutive rows, so every reduction instruction covers
+// 256 contiguous bytes.  Only m < M, n < N are written; P must be zero there
+// on entry, and the kernel that reads it clears it.  The grid is persistent
+// (items round-robin over the CTAs): the tile counts come from device-side
+// sizes (the spectrum window).
 // Every wait is bounded; a wait that runs out sets the error bit, each role
 // stops, the CTA waits (bounded) for what it issued, frees its tensor memory
 // and returns.  Single-GPU code: no multicast.
@@ -60,8 +61,9 @@ constexpr int kLevels = 8;       // levels L = i + j <= 7
 constexpr int BM = 128;
 constexpr int BN = 64;
 constexpr int BK = 64;           // bf16 values per K tile: one 128-byte swizzle row
-constexpr int kThreads = 192;    // producer warp, MMA warp, four epilogue warps
-constexpr int kMaxK = 1023 * BK; // K tiles whose integer sums stay below 2^53
+constexpr int kEpiWarps = 8;     // two per TMEM lane quarter
+constexpr int kThreads = 64 + 32 * kEpiWarps;  // producer warp, MMA warp, epilogue warps
+constexpr int kMaxK = 32 * BK;   // K tiles whose integer sums stay below 2^62
 constexpr int kABytes = BM * BK * 2;  // one A plane tile
 constexpr int kBBytes = BN * BK * 2;  // one B plane tile
 constexpr int kSmem = 1024 + kPlanes * (kABytes + kBBytes) + 256;
@@ -71,8 +73,8 @@ constexpr int kTmemCols = kLevels * BN;  // 512
 // window): rows = min(*m_dev, m_max) when m_dev is set, columns =
 // min(*n_dev, n_max) when n_dev is set; with win_r0/win_W the rows (win_rows)
 // or the columns number at most 1 + the largest |r - N/2| over the window
-// rows.  The output is compact for those sizes: P[(h * N + n) * ldm + m] with
-// ldm = M rounded up to 32 (Dims below).
+// rows.  The output is compact for those sizes: P[n * ldm + m] with ldm = M
+// rounded up to 32 (Dims below).
 struct Params {
     int m_max, n_max, K;
     const int* m_dev;            // rows from the device, or null
@@ -81,7 +83,7 @@ struct Params {
     const int* win_W;
     int win_rows;                // the window bounds the rows (1) or the columns (0)
     int half;                    // N/2 of the image
-    long long* P;                // hi / lo sums (zero on entry where m < M, n < N)
+    long long* P;                // integer sums in units of 2^-35 (zero on entry where m < M, n < N)
     unsigned* err;
 };
 struct Dims {
@@ -145,9 +147,21 @@ __device__ __forceinline__ void tmem_wait64(uint32_t* r) {
                  :
                  : "memory");
 }
-// the product sum_L 2^(-7L) lev_L from the two integer sums (one rounding)
-__host__ __device__ inline double combine_hi_lo(long long hi, long long lo) {
-    return fma((double)lo, 0x1p-49, (double)hi * 0x1p-21);
+// sum_L 2^(-7L) lev_L from the integer sum V (units of 2^-35; one rounding)
+__host__ __device__ inline double combine_levels(long long v) { return (double)v * 0x1p-35; }
+// V of one element of one K tile from its eight (exact, integer) FP32 levels
+__host__ __device__ inline long long level_int(float x) {  // |x| < 2^24, an integer
+#ifdef __CUDA_ARCH__
+    return (long long)__float2int_rz(x);
+#else
+    return (long long)x;
+#endif
+}
+__host__ __device__ inline long long fold_levels(const float* lev) {
+    long long v = 0;
+    for (int L = 0; L < 6; ++L) v = v * 128 + level_int(lev[L]);
+    const long long tail = level_int(lev[6]) * 128 + level_int(lev[7]);
+    return v + ((tail + 8192) >> 14);
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
@@ -162,7 +176,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint64_t* full = bars;                 // [kPlanes] plane i of A and B landed
     uint64_t* empty = bars + kPlanes;      // every MMA of the item has read shared memory
     uint64_t* accf = bars + kPlanes + 1;   // the item's levels are in tensor memory
-    uint64_t* acce = bars + kPlanes + 2;   // the epilogue has read them (128 arrivals)
+    uint64_t* acce = bars + kPlanes + 2;   // the epilogue has read them (one arrival per epilogue thread)
     uint64_t* done = bars + kPlanes + 3;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kPlanes + 4);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
@@ -177,7 +191,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int s = 0; s < kPlanes; ++s) mbar_init(&full[s], 1);
         mbar_init(empty, 1);
         mbar_init(accf, 1);
-        mbar_init(acce, 128);
+        mbar_init(acce, 32 * kEpiWarps);
         mbar_init(done, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -285,9 +299,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (!mbar_wait(done, 0u)) fail();  // every MMA complete before the tensor memory is freed
         }
     } else {
-        // ---- epilogue: lane = tile row; 8 levels of 8 columns at a time,
-        // folded into the hi / lo integer sums of each element
-        const int quarter = warp & 3;
+        // ---- epilogue: lane = tile row; warp w reads TMEM lane quarter w % 4
+        // and columns [32 h, 32 h + 32), h = (w - 2) / 4; 8 levels of 8
+        // columns at a time, folded into one integer per element
+        const int quarter = warp & 3, half = (warp - 2) >> 2;
         const uint32_t lane_off = (uint32_t)(quarter * 32) << 16;
         int t = 0;
         for (int item = blockIdx.x; item < items; item += gridDim.x, ++t) {
@@ -301,10 +316,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int row = m0 + quarter * 32 + lane;
             (void)kt;
             const bool live = row < dm.M;
-            long long* hi_row = p.P + row;
-            long long* lo_row = p.P + (long long)dm.N * dm.ldm + row;
+            long long* out_row = p.P + row;
 #pragma unroll 1
-            for (int c0 = 0; c0 < BN; c0 += 8) {
+            for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 8) {
                 uint32_t x[kLevels * 8];
 #pragma unroll
                 for (int L = 0; L < kLevels; ++L) tmem_ld8_async(tmem + lane_off + (uint32_t)(L * BN + c0), x + 8 * L);
@@ -312,15 +326,11 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                 for (int c = 0; c < 8; ++c) {
                     const int n = n0 + c0 + c;
-                    long long hi = 0, lo = 0;
+                    float lev[kLevels];
 #pragma unroll
-                    for (int L = 0; L < 4; ++L) hi = hi * 128 + (long long)__float2int_rz(__uint_as_float(x[8 * L + c]));
-#pragma unroll
-                    for (int L = 4; L < 8; ++L) lo = lo * 128 + (long long)__float2int_rz(__uint_as_float(x[8 * L + c]));
-                    if (live && n < dm.N) {
-                        red_add_u64(hi_row + (long long)n * dm.ldm, hi);
-                        red_add_u64(lo_row + (long long)n * dm.ldm, lo);
-                    }
+                    for (int L = 0; L < kLevels; ++L) lev[L] = __uint_as_float(x[8 * L + c]);
+                    const long long v = fold_levels(lev);
+                    if (live && n < dm.N) red_add_u64(out_row + (long long)n * dm.ldm, v);
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

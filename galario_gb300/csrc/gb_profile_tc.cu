@@ -18,7 +18,7 @@
 // products on the bf16 tensor cores (gb_ozaki.cuh): each operand row as eight
 // balanced base-128 digits relative to the row's exponent, the 36 digit-pair
 // products with i + j <= 7 summed exactly in integer levels and folded into
-// two exact 64-bit integer sums per element.
+// one 64-bit integer sum per element.
 //
 // Passes (one stream, no host round trip; K, r0, W come from the device
 // window written by the extent pass):
@@ -81,13 +81,12 @@ __device__ __forceinline__ void write_digits(const double* v, int n, int e, unsi
     }
 }
 
-// sum_L 2^(-7 L) lev_L of one product element from its hi / lo integer sums
-// (see ozaki_levels_kernel), clearing them for the next call
-__device__ __forceinline__ double take_sum(long long* __restrict__ hi, long long lo_off) {
-    const long long h = hi[0], l = hi[lo_off];
-    hi[0] = 0;
-    hi[lo_off] = 0;
-    return oz::combine_hi_lo(h, l);
+// sum_L 2^(-7 L) lev_L of one product element from its integer sum (see
+// ozaki_levels_kernel), clearing it for the next call
+__device__ __forceinline__ double take_sum(long long* __restrict__ p) {
+    const long long v = *p;
+    *p = 0;
+    return oz::combine_levels(v);
 }
 
 // x 2^n from exponent-field arithmetic (exact while the result is a normal number)
@@ -140,7 +139,6 @@ __global__ void __launch_bounds__(kFoldThreads) oz_mid_kernel(oz::Params p, cons
                                                               int* __restrict__ ed) {
     __shared__ double red[kFoldThreads / 32];
     const oz::Dims dm = oz::item_dims(p);  // M = nF rows (a), N = K columns (k)
-    const long long lo_off = (long long)dm.N * dm.ldm;
     for (int k = blockIdx.x; k < dm.N; k += gridDim.x) {
         const int eck = ec[k];
         double v[kPerThread];
@@ -150,7 +148,7 @@ __global__ void __launch_bounds__(kFoldThreads) oz_mid_kernel(oz::Params p, cons
             const int a = threadIdx.x + kFoldThreads * i;
             v[i] = 0.0;
             if (a < nF) {
-                const double acc = take_sum(p.P + (long long)k * dm.ldm + a, lo_off);
+                const double acc = take_sum(p.P + (long long)k * dm.ldm + a);
                 const int ea = ef[a];
                 v[i] = (ea == kBadRow || eck == kBadRow) ? (double)NAN : scale2(acc, eck + ea - 12);
                 const double m = fabs(v[i]);
@@ -174,12 +172,12 @@ __global__ void __launch_bounds__(256) oz_out_kernel(oz::Params p, const int* __
                                                      double* __restrict__ amp, long long s_row, long long s_col) {
     const oz::Dims dm = oz::item_dims(p);  // M = T + 1 rows (t), N = K columns (k)
     const Window w = get_window(-1, -1, -1, st);
-    const long long lo_off = (long long)dm.N * dm.ldm;
-    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < lo_off;
+    const long long total = (long long)dm.N * dm.ldm;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += (long long)gridDim.x * blockDim.x) {
         const int k = (int)(e / dm.ldm), t = (int)(e - (long long)k * dm.ldm);
         if (t >= dm.M) continue;
-        const double acc = take_sum(p.P + e, lo_off);
+        const double acc = take_sum(p.P + e);
         const int ek = ed[k];
         const double f = ek == kBadRow ? (double)NAN : scale2(acc, ek + ec[t] - 12);
 #pragma unroll
@@ -250,7 +248,8 @@ bool profile_tc_ok(int N, int rmax) {
     const char* v = std::getenv("GALARIO_TC");
     if (v && v[0] == '0') return false;
     const int nF = profile_tc_quadrant(N, rmax);
-    return N >= 16 && N % 2 == 0 && N <= 16384 && nF >= 1 && nF <= kMaxRow && tc::encode_fn() != nullptr;
+    return N >= 16 && N % 2 == 0 && N <= 16384 && nF >= 1 && nF <= kMaxRow && nF <= oz::kMaxK &&
+           tc::encode_fn() != nullptr;
 }
 
 // the digits of C[j][c] = w_c cos(2 pi c j / N), j <= N/2, c < nF (cosines
@@ -311,8 +310,8 @@ static cudaError_t prepare(ProfileTc* t, int N, int nF) {
     if (e == cudaSuccess) e = t->dd.get(sizeof(unsigned short) * oz::kPlanes * planeD, true, &fresh);
     moved |= fresh;
     if (e == cudaSuccess) e = t->ed.get(sizeof(int) * C, false, &fresh);
-    if (e == cudaSuccess) e = t->p1.get(sizeof(long long) * 2 * (size_t)ldmF * C, true, &fresh);
-    if (e == cudaSuccess) e = t->p2.get(sizeof(long long) * 2 * (size_t)ldmC * C, true, &fresh);
+    if (e == cudaSuccess) e = t->p1.get(sizeof(long long) * (size_t)ldmF * C, true, &fresh);
+    if (e == cudaSuccess) e = t->p2.get(sizeof(long long) * (size_t)ldmC * C, true, &fresh);
     if (e != cudaSuccess) return e;
     if (moved || !t->maps) {
         t->maps = oz::make_map(&t->map_ca, t->cd.p, nF, C, ldF, planeD, oz::BM) &&

@@ -1,12 +1,12 @@
 // Unit test of the bf16 tensor-core digit products (galario_gb300/csrc/gb_ozaki.cuh).
 //
 // 1. Exactness: random integer digit planes (|d| <= 64) for A (M x K) and
-//    B (N x K); the kernel's two integer sums per element,
-//    hi = sum_{L<4} 2^(7(3-L)) lev_L and lo = sum_{4<=L<8} 2^(7(7-L)) lev_L
-//    with lev_L = sum_{i+j=L} sum_k A_i B_j, must equal the int64 result
-//    exactly, including M, N, K that are not multiples of the tiles (zero
-//    fill), every digit at +-64 (the largest level sums of a K tile) and K of
-//    many tiles.
+//    B (N x K); the kernel's integer sum per element, the sum over its K
+//    tiles of V = sum_{L<=5} 2^(7(5-L)) lev_L + round((2^7 lev_6 + lev_7) / 2^14)
+//    with lev_L = sum_{i+j=L} sum_{k in the tile} A_i B_j, must equal the
+//    int64 result exactly, including M, N, K that are not multiples of the
+//    tiles (zero fill), every digit at +-64 (the largest level sums of a K
+//    tile) and K of many tiles.
 // 2. FP64 products: random doubles with rows of widely different scales, the
 //    digits of digits8, the kernel, and the sums combined in double;
 //    compared with a long double product, the error must stay below
@@ -57,7 +57,7 @@ struct Planes {
     }
 };
 
-// the kernel's sums on the GPU: P[(h * N + n) * ldm + m], h = 0 (hi), 1 (lo)
+// the kernel's sums on the GPU: P[n * ldm + m]
 static std::vector<long long> run_levels(const Planes& A, const Planes& B, oz::Dims* dims) {
     CUtensorMap am, bm;
     if (!oz::make_map(&am, A.d, A.K, A.rows, A.ld, (long long)A.rows * A.ld, oz::BM) ||
@@ -68,7 +68,7 @@ static std::vector<long long> run_levels(const Planes& A, const Planes& B, oz::D
     const oz::Dims dm = oz::dims_of(A.rows, B.rows);
     long long* P = nullptr;
     unsigned* err = nullptr;
-    const size_t np = (size_t)2 * dm.N * dm.ldm;
+    const size_t np = (size_t)dm.N * dm.ldm;
     CK(cudaMalloc(&P, np * 8));
     CK(cudaMemset(P, 0, np * 8));
     CK(cudaMalloc(&err, 4));
@@ -116,24 +116,29 @@ static int exact_case(int M, int N, int K, bool extreme, unsigned seed) {
     long long bad = 0, maxabs = 0;
     for (int m = 0; m < M; ++m)
         for (int n = 0; n < N; ++n) {
-            long long lev[oz::kLevels] = {0};
-            for (int L = 0; L < oz::kLevels; ++L)
-                for (int i = 0; i <= L; ++i) {
-                    const int j = L - i;
-                    if (i >= oz::kPlanes || j >= oz::kPlanes) continue;
-                    for (int k = 0; k < K; ++k) lev[L] += (long long)A.v[A.at(i, m, k)] * B.v[B.at(j, n, k)];
+            long long want = 0;
+            for (int k0 = 0; k0 < K; k0 += oz::BK) {  // one K tile at a time, as the kernel folds them
+                float lev[oz::kLevels];
+                for (int L = 0; L < oz::kLevels; ++L) {
+                    long long l = 0;
+                    for (int i = 0; i <= L; ++i) {
+                        const int j = L - i;
+                        if (i >= oz::kPlanes || j >= oz::kPlanes) continue;
+                        for (int k = k0; k < std::min(K, k0 + oz::BK); ++k)
+                            l += (long long)A.v[A.at(i, m, k)] * B.v[B.at(j, n, k)];
+                    }
+                    maxabs = std::max(maxabs, std::llabs(l));
+                    lev[L] = (float)l;  // below 2^24: exact
                 }
-            long long hi = 0, lo = 0;
-            for (int L = 0; L < 4; ++L) hi = hi * 128 + lev[L];
-            for (int L = 4; L < 8; ++L) lo = lo * 128 + lev[L];
-            for (int L = 0; L < oz::kLevels; ++L) maxabs = std::max(maxabs, std::llabs(lev[L]));
-            const long long ghi = P[(size_t)n * dm.ldm + m], glo = P[((size_t)dm.N + n) * dm.ldm + m];
-            if (ghi != hi || glo != lo) {
-                if (bad < 5) std::printf("  (%d, %d): got (%lld, %lld) want (%lld, %lld)\n", m, n, ghi, glo, hi, lo);
+                want += oz::fold_levels(lev);
+            }
+            const long long got = P[(size_t)n * dm.ldm + m];
+            if (got != want) {
+                if (bad < 5) std::printf("  (%d, %d): got %lld want %lld\n", m, n, got, want);
                 ++bad;
             }
         }
-    std::printf("exact M=%d N=%d K=%d%s: %lld mismatches, max |level| %lld (2^%.1f)\n", M, N, K,
+    std::printf("exact M=%d N=%d K=%d%s: %lld mismatches, max |level of a K tile| %lld (2^%.1f)\n", M, N, K,
                 extreme ? " (every digit 64)" : "", bad, maxabs, std::log2((double)maxabs));
     return bad == 0 ? 0 : 1;
 }
@@ -174,7 +179,7 @@ static int fp64_case(int M, int N, int K, unsigned seed) {
     double worst = 0;
     for (int m = 0; m < M; ++m)
         for (int n = 0; n < N; ++n) {
-            const double acc = oz::combine_hi_lo(P[(size_t)n * dm.ldm + m], P[((size_t)dm.N + n) * dm.ldm + m]);
+            const double acc = oz::combine_levels(P[(size_t)n * dm.ldm + m]);
             const double got = std::ldexp(acc, ea[m] + eb[n] - 12);
             long double ref = 0, amax = 0, bmax = 0;
             for (int k = 0; k < K; ++k) {
