@@ -851,7 +851,12 @@ __device__ __forceinline__ bool interp_cell_real(const typename Launch<T>::VisAr
         const T zr = fma(q, fma(t, (yr[2] - yr[3]) - f1, f3), fma(t, f1, yr[0]));
         neg = zr < (T)0;
     }
-    *out = neg ? -amp : amp;
+    if constexpr (sizeof(T) == 8) {
+        // the sign as a bit operation (no FP64 instruction)
+        *out = __longlong_as_double(__double_as_longlong(amp) ^ (neg ? (long long)0x8000000000000000ULL : 0LL));
+    } else {
+        *out = neg ? -amp : amp;
+    }
     return true;
 }
 
@@ -1579,7 +1584,10 @@ cudaError_t Launch<T>::cols(const CT* zt, int N, int band0, int band1, const CT*
 
 template <typename T> int Launch<T>::vis_grid(int nd) {
     int blocks = (nd + 255) / 256;
-    const int cap = num_sms() * 8;
+    // FP64: one wave of the profile kernel (4 blocks per SM), so that every
+    // thread's share of the block reduction's FP64 additions is spread over
+    // twice as many visibilities
+    const int cap = num_sms() * (sizeof(T) == 8 ? 4 : 8);
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
     return blocks;

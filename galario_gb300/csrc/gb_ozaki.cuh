@@ -182,10 +182,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const Dims dm = item_dims(p);
-    const int mt_n = dm.Mp / BM, nt_n = (dm.N + BN - 1) / BN, kt_n = (p.K + BK - 1) / BK;
-    const int items = mt_n * nt_n * kt_n;
-    if ((int)blockIdx.x >= items) return;  // uniform: nothing allocated yet
+    // the next kernel of the stream (launched as a programmatic dependent)
+    // may start its set-up now; it reads this kernel's output only after its
+    // griddepcontrol.wait, which waits for this grid to complete
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kPlanes; ++s) mbar_init(&full[s], 1);
@@ -206,6 +206,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
+    // launched as a programmatic dependent of the kernel before it: the set-up
+    // above overlaps that kernel's tail; its outputs (the operands, the
+    // window sizes) are read only after this wait (a no-op otherwise)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    const Dims dm = item_dims(p);
+    const int mt_n = dm.Mp / BM, nt_n = (dm.N + BN - 1) / BN, kt_n = (p.K + BK - 1) / BK;
+    const int items = mt_n * nt_n * kt_n;  // CTAs past it only free their tensor memory
     auto fail = [&]() {
         atomicOr(p.err, kErrSpin);
         *abort_flag = 1;

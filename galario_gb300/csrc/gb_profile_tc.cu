@@ -138,6 +138,8 @@ __global__ void __launch_bounds__(kFoldThreads) oz_mid_kernel(oz::Params p, cons
                                                               long long planeD, unsigned short* __restrict__ dd,
                                                               int* __restrict__ ed) {
     __shared__ double red[kFoldThreads / 32];
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");  // the second product may set up
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // programmatic dependent of the first product
     const oz::Dims dm = oz::item_dims(p);  // M = nF rows (a), N = K columns (k)
     for (int k = blockIdx.x; k < dm.N; k += gridDim.x) {
         const int eck = ec[k];
@@ -170,6 +172,7 @@ __global__ void __launch_bounds__(256) oz_out_kernel(oz::Params p, const int* __
                                                      const int* __restrict__ ec, int N,
                                                      const DevState* __restrict__ st, C2<double>* __restrict__ out,
                                                      double* __restrict__ amp, long long s_row, long long s_col) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // programmatic dependent of the product
     const oz::Dims dm = oz::item_dims(p);  // M = T + 1 rows (t), N = K columns (k)
     const Window w = get_window(-1, -1, -1, st);
     const long long total = (long long)dm.N * dm.ldm;
@@ -220,6 +223,25 @@ struct Buf {
 };
 
 inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+// Launch as a programmatic dependent of the stream's previous kernel: its
+// CTAs may start (and run up to griddepcontrol.wait) while that kernel's last
+// CTAs finish, which hides the gap between the short passes of the chain.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_dependent(void (*kern)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
+                             Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
 
 }  // namespace
 
@@ -354,13 +376,14 @@ cudaError_t profile_tc_window(ProfileTc* t, int N, DevState* st, C2<double>* out
     p1.half = N / 2;
     p1.P = static_cast<long long*>(t->p1.p);
     p1.err = &st->err;
+    // an ordinary launch: the stream's previous operations include the join
+    // with the extent pass, whose window this product reads
     oz::ozaki_levels_kernel<<<grid, oz::kThreads, oz::kSmem, s>>>(t->map_f, t->map_cb, p1);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    oz_mid_kernel<<<2 * grid, kFoldThreads, 0, s>>>(p1, static_cast<const int*>(t->ec.p),
-                                                     static_cast<const int*>(t->ef.p), nF, ldF, (long long)C * ldF,
-                                                     static_cast<unsigned short*>(t->dd.p), static_cast<int*>(t->ed.p));
-    e = cudaGetLastError();
+    e = launch_dependent(oz_mid_kernel, 2 * grid, kFoldThreads, 0, s, p1, static_cast<const int*>(t->ec.p),
+                         static_cast<const int*>(t->ef.p), nF, ldF, (long long)C * ldF,
+                         static_cast<unsigned short*>(t->dd.p), static_cast<int*>(t->ed.p));
     if (e != cudaSuccess) return e;
     // S'^T = C[0:T+1] D1^T: rows t <= T (the window rows' distances), columns k < K
     oz::Params p2{};
@@ -374,11 +397,12 @@ cudaError_t profile_tc_window(ProfileTc* t, int N, DevState* st, C2<double>* out
     p2.half = N / 2;
     p2.P = static_cast<long long*>(t->p2.p);
     p2.err = &st->err;
-    oz::ozaki_levels_kernel<<<grid, oz::kThreads, oz::kSmem, s>>>(t->map_ca, t->map_d, p2);
-    e = cudaGetLastError();
+    e = launch_dependent(oz::ozaki_levels_kernel, grid, oz::kThreads, (size_t)oz::kSmem, s, t->map_ca, t->map_d, p2);
     if (e != cudaSuccess) return e;
-    oz_out_kernel<<<2 * grid, 256, 0, s>>>(p2, static_cast<const int*>(t->ed.p), static_cast<const int*>(t->ec.p), N,
-                                           st, out, amp, s_row, s_col);
+    e = launch_dependent(oz_out_kernel, 2 * grid, 256, 0, s, p2, static_cast<const int*>(t->ed.p),
+                         static_cast<const int*>(t->ec.p), N, static_cast<const DevState*>(st), out, amp, s_row,
+                         s_col);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
