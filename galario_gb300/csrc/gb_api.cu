@@ -511,9 +511,12 @@ template <typename T> struct Pipe {
         });
         // a swept profile's spectrum is real: 4 real corners per cell record
         const bool real_spec = img == nullptr;
+        // the tensor-core chain's last passes, the cell records and the
+        // visibility pass follow one another on s: programmatic dependents
+        const bool pdl = tc_prof && !ov && !before_vis && !c.timing;  // no event records between the kernels
         timed(c, s, ST_QUAD, [&] {
             if (real_spec)
-                CK(L::quads_real(win, 1, N, C, st, quads, qcap, s));
+                CK(L::quads_real(win, 1, N, C, st, quads, qcap, s, pdl));
             else
                 CK(L::quads(win, amp, 1, N, C, st, quads, qcap, -1, -1, -1, s));
         });
@@ -594,7 +597,7 @@ template <typename T> struct Pipe {
             CK(cudaEventRecord(c.ev_vis2, c.vis2));
             CK(cudaStreamWaitEvent(s, c.ev_vis2, 0));
         } else if (nd > 0) {
-            timed(c, s, ST_VIS, [&] { CK(L::vis(a, s)); });
+            timed(c, s, ST_VIS, [&] { CK(L::vis(a, s, pdl)); });
         }
     }
 };

@@ -194,7 +194,9 @@ template <typename T> struct Launch {
         int part_off = 0;
         int parts_total = 0;
     };
-    static cudaError_t vis(const VisArgs& a, cudaStream_t s);
+    // pdl: launch as a programmatic dependent of the stream's previous kernel
+    // (the kernels wait with griddepcontrol.wait before reading its output)
+    static cudaError_t vis(const VisArgs& a, cudaStream_t s, bool pdl = false);
     // Cell-major copy of the window for the visibility gather: one record of
     // QUAD_REC reals per cell (k, r), k in [0, K), r in [r0, r0 + W), at
     // quads + (k * W + (r - r0)) * QUAD_REC, holding the cell's 4 bilinear
@@ -211,7 +213,7 @@ template <typename T> struct Launch {
     // bytes); FP64, the 4 coefficients of the bilinear modulus and the 4
     // corners as FP32 (48 bytes; see quad_real_kernel)
     static cudaError_t quads_real(const CT* spec, long long s_row, long long s_col, int C, const DevState* state,
-                                  T* quads, long long cap, cudaStream_t s);
+                                  T* quads, long long cap, cudaStream_t s, bool pdl = false);
     static int vis_grid(int nd);
     // expert-stage kernels
     static cudaError_t fftshift_real(T* padded, int N, cudaStream_t s);

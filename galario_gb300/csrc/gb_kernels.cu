@@ -39,6 +39,24 @@ namespace gbg {
 
 namespace {
 
+// Launch on s; with pdl as a programmatic dependent of the stream's previous
+// kernel (its CTAs may start while that kernel finishes; the kernel's
+// griddepcontrol.wait precedes every read of the previous kernel's output).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_on(void (*kern)(KArgs...), int grid, int block, cudaStream_t s, bool pdl, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // ---------------------------------------------------------------------------
 // row pass kernels
 // ---------------------------------------------------------------------------
@@ -1071,6 +1089,7 @@ template <typename T, bool CHI2, bool VISOUT, bool REALQ, bool SPLIT = false>
 __global__ void __launch_bounds__(256, (sizeof(T) == 8 && REALQ) ? 4 : 1) vis_kernel(typename Launch<T>::VisArgs a) {
     using CT = C2<T>;
     __shared__ double sh[32];
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // a no-op unless launched as a programmatic dependent
     const Window w = get_window(a.host_K, a.host_r0, a.host_W, a.state);
     T acc = (T)0;
     unsigned err = 0u;
@@ -1177,6 +1196,7 @@ __global__ void quad_kernel(const C2<T>* __restrict__ spec, const T* __restrict_
 template <typename T>
 __global__ void quad_real_kernel(const C2<T>* __restrict__ spec, long long s_row, long long s_col, int C,
                                  const DevState* __restrict__ st, T* __restrict__ quads, long long cap) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // a no-op unless launched as a programmatic dependent
     const Window w = get_window(-1, -1, -1, st);
     const long long ncell = (long long)w.K * w.W;
     if (ncell > cap) return;  // the visibility pass gathers from spec/amp instead
@@ -1593,7 +1613,7 @@ template <typename T> int Launch<T>::vis_grid(int nd) {
     return blocks;
 }
 
-template <typename T> cudaError_t Launch<T>::vis(const VisArgs& args, cudaStream_t s) {
+template <typename T> cudaError_t Launch<T>::vis(const VisArgs& args, cudaStream_t s, bool pdl) {
     VisArgs a = args;
     a.finalize();
     const int blocks = vis_grid(a.nd);
@@ -1607,9 +1627,9 @@ template <typename T> cudaError_t Launch<T>::vis(const VisArgs& args, cudaStream
         return cudaGetLastError();
     }
     if (a.real_quads && a.quads) {
-        if (chi2 && vo) vis_kernel<T, true, true, true><<<blocks, 256, 0, s>>>(a);
-        else if (chi2) vis_kernel<T, true, false, true><<<blocks, 256, 0, s>>>(a);
-        else vis_kernel<T, false, true, true><<<blocks, 256, 0, s>>>(a);
+        if (chi2 && vo) return launch_on(vis_kernel<T, true, true, true>, blocks, 256, s, pdl, a);
+        else if (chi2) return launch_on(vis_kernel<T, true, false, true>, blocks, 256, s, pdl, a);
+        else return launch_on(vis_kernel<T, false, true, true>, blocks, 256, s, pdl, a);
     } else {
         if (chi2 && vo) vis_kernel<T, true, true, false><<<blocks, 256, 0, s>>>(a);
         else if (chi2) vis_kernel<T, true, false, false><<<blocks, 256, 0, s>>>(a);
@@ -1620,9 +1640,8 @@ template <typename T> cudaError_t Launch<T>::vis(const VisArgs& args, cudaStream
 
 template <typename T>
 cudaError_t Launch<T>::quads_real(const CT* spec, long long s_row, long long s_col, int C, const DevState* state,
-                                  T* q, long long cap, cudaStream_t s) {
-    quad_real_kernel<T><<<num_sms() * 4, 256, 0, s>>>(spec, s_row, s_col, C, state, q, cap);
-    return cudaGetLastError();
+                                  T* q, long long cap, cudaStream_t s, bool pdl) {
+    return launch_on(quad_real_kernel<T>, num_sms() * 4, 256, s, pdl, spec, s_row, s_col, C, state, q, cap);
 }
 
 template <typename T>
