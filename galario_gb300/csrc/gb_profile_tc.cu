@@ -14,14 +14,15 @@
 // window row r takes S'[.][|r - N/2|].  Both run transposed (D1^T = F C^T,
 // S'^T = C D1^T), so that the row of D1 that the next pass splits, and the
 // column of S' that becomes a window column, are contiguous in the products'
-// output (whose fastest index is the row of the first factor).  Both products run as FP64-grade
-// products on the bf16 tensor cores (gb_ozaki.cuh): each operand row as eight
-// balanced base-128 digits relative to the row's exponent, the 36 digit-pair
-// products with i + j <= 7 summed exactly in integer levels and folded into
-// one 64-bit integer sum per element.
+// output (whose fastest index is the row of the first factor).  Both are
+// FP64-grade products on the bf16 tensor cores (gb_ozaki.cuh): each operand
+// row as eight balanced base-128 digits relative to the row's exponent, the
+// 36 digit-pair products with i + j <= 7 summed exactly in integer levels
+// and folded into one 64-bit integer sum per element.
 //
-// Passes (one stream, no host round trip; K, r0, W come from the device
-// window written by the extent pass):
+// Passes (no host round trip; K, r0, W come from the device window written
+// by the extent pass, which runs on a side stream beside the fold; the
+// passes after the first product are programmatic dependent launches):
 //   oz_fold_kernel       the quadrant of the sweep (reference sweep_core
 //                        :1048-1071, central pixel :1136-1153), one row per
 //                        block, its row exponent and digits
