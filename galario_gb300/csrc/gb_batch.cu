@@ -1188,14 +1188,18 @@ __global__ void sweep_fold_kernel(Geo g, const float* __restrict__ intensity, co
     flo[o] = tc::tf32_rna(x - hi);
 }
 
-// Cell gradients of a real window -> the window gradient as a TF32 pair (the
-// tensor-core path's spectrum carries no sign folding); grid (K, B)
+// Cell gradients of a real window -> the window gradient, folded over the
+// mirror rows: G'[k][t] = G[k][h0 - t] + G[k][h0 + t] (h0 = N/2 - r0, the
+// terms inside the window), t < T1, as a TF32 pair (the tensor-core path's
+// spectrum carries no sign folding); grid (K, B).  The spectrum is even
+// about row N/2, so its adjoint needs only the folded gradient.
 __global__ void quadT_real_tc_kernel(Geo g, const float* __restrict__ cgrad4, const float* __restrict__ wr,
-                                     float* __restrict__ ghi, float* __restrict__ glo, int ldW) {
+                                     float* __restrict__ ghi, float* __restrict__ glo, int T1, int ldT) {
     const long long ncell = (long long)g.K * g.W;
     const int k = blockIdx.x, b = blockIdx.y;
+    const int h0 = g.N / 2 - g.r0;
     const float* cg = cgrad4 + (size_t)b * ncell * 4;
-    for (int q = threadIdx.x; q < g.W; q += blockDim.x) {
+    auto grad_at = [&](int q) {  // dchi2 / dS[k][q]
         float ga = 0.f;
         auto take = [&](int kc, int qc, int c) {
             if (kc < 0 || qc < 0 || kc >= g.K || qc >= g.W) return;
@@ -1207,9 +1211,14 @@ __global__ void quadT_real_tc_kernel(Geo g, const float* __restrict__ cgrad4, co
         take(k - 1, q, 3);
         const float y = wr[(size_t)b * ncell + (size_t)k * g.W + q];
         ga *= 2.f;  // the vis pass records halves of dchi2/dA
-        const float gy = y < 0.f ? -ga : (y > 0.f ? ga : 0.f);
+        return y < 0.f ? -ga : (y > 0.f ? ga : 0.f);
+    };
+    for (int t = threadIdx.x; t < T1; t += blockDim.x) {
+        const int q1 = h0 - t, q2 = h0 + t;
+        float gy = (q1 >= 0 && q1 < g.W) ? grad_at(q1) : 0.f;
+        if (t > 0 && q2 >= 0 && q2 < g.W) gy += grad_at(q2);
         const float hi = tc::tf32_rna(gy);
-        const size_t o = ((size_t)b * g.K + k) * ldW + q;
+        const size_t o = ((size_t)b * g.K + k) * ldT + t;
         ghi[o] = hi;
         glo[o] = tc::tf32_rna(gy - hi);
     }
@@ -1554,10 +1563,11 @@ constexpr size_t kMaxGraphs = 32;
 // cosine matrices of the tensor-core spectrum passes (one geometry) as TF32
 // pairs in device memory; row-major with the leading dimensions below
 struct CosMats {
-    int ldF = 0, ldW = 0, ldK = 0;
+    int ldF = 0, ldT = 0, ldK = 0;
+    int T1 = 0;                                  // distinct |r - N/2| over the window rows: 0 .. T1 - 1
     float *ck_hi = nullptr, *ck_lo = nullptr;    // Ck   [K][ldF]
-    float *cv_hi = nullptr, *cv_lo = nullptr;    // Cv   [W][ldF]
-    float *cvt_hi = nullptr, *cvt_lo = nullptr;  // Cv^T [rmax+1][ldW]
+    float *cv_hi = nullptr, *cv_lo = nullptr;    // Cv   [T1][ldF]: row t = w_a cos(2 pi a t / N)
+    float *cvt_hi = nullptr, *cvt_lo = nullptr;  // Cv^T [rmax+1][ldT]
     float *ckt_hi = nullptr, *ckt_lo = nullptr;  // Ck^T [rmax+1][ldK]
 };
 inline int round4(int x) { return (x + 3) / 4 * 4; }
@@ -1586,14 +1596,15 @@ struct BatchWs {
         const int n = rmax + 1;
         CosMats m;
         m.ldF = round4(n);
-        m.ldW = round4(W);
+        m.T1 = std::max(N / 2 - r0, r0 + W - 1 - N / 2) + 1;
+        m.ldT = round4(m.T1);
         m.ldK = round4(K);
         const long double two_pi = 6.283185307179586476925286766559005768L;
         auto wgt = [&](int j) { return (j == 0 || 2 * j == N) ? 1.0L : 2.0L; };
         auto cosn = [&](long long p) { return cosl(two_pi * (long double)(p % N) / (long double)N); };
         std::vector<float> ckh((size_t)K * m.ldF, 0.f), ckl(ckh.size(), 0.f);
-        std::vector<float> cvh((size_t)W * m.ldF, 0.f), cvl(cvh.size(), 0.f);
-        std::vector<float> cvth((size_t)n * m.ldW, 0.f), cvtl(cvth.size(), 0.f);
+        std::vector<float> cvh((size_t)m.T1 * m.ldF, 0.f), cvl(cvh.size(), 0.f);
+        std::vector<float> cvth((size_t)n * m.ldT, 0.f), cvtl(cvth.size(), 0.f);
         std::vector<float> ckth((size_t)n * m.ldK, 0.f), cktl(ckth.size(), 0.f);
         auto put = [](std::vector<float>& h, std::vector<float>& l, size_t i, long double x) {
             const float f = (float)x;
@@ -1606,12 +1617,11 @@ struct BatchWs {
                 put(ckh, ckl, (size_t)k * m.ldF + c, x);
                 put(ckth, cktl, (size_t)c * m.ldK + k, x);
             }
-        for (int q = 0; q < W; ++q) {
-            const int rr = std::abs(r0 + q - N / 2);
+        for (int t = 0; t < m.T1; ++t) {  // the spectrum is even about row N/2: one row per |r - N/2|
             for (int a = 0; a < n; ++a) {
-                const long double x = wgt(a) * cosn((long long)a * rr);
-                put(cvh, cvl, (size_t)q * m.ldF + a, x);
-                put(cvth, cvtl, (size_t)a * m.ldW + q, x);
+                const long double x = wgt(a) * cosn((long long)a * t);
+                put(cvh, cvl, (size_t)t * m.ldF + a, x);
+                put(cvth, cvtl, (size_t)a * m.ldT + t, x);
             }
         }
         auto up = [](const std::vector<float>& h) {
@@ -2189,7 +2199,7 @@ static void batch_run(const BatchCall& call) {
             tF = ws.tcF.get<float>((size_t)2 * B * nF * cm->ldF);
             tD1 = ws.tcD1.get<float>((size_t)2 * B * g.K * cm->ldF);
             if (grad) {
-                tG = ws.tcG.get<float>((size_t)2 * B * g.K * cm->ldW);
+                tG = ws.tcG.get<float>((size_t)2 * B * g.K * cm->ldT);
                 tG1 = ws.tcG1.get<float>((size_t)2 * B * nF * cm->ldK);
                 tGF = ws.tcGF.get<float>((size_t)B * nF * cm->ldF);
                 const size_t nchunk = (size_t)(nF + kRowsPerCta - 1) / kRowsPerCta;
@@ -2348,7 +2358,8 @@ static void batch_run(const BatchCall& call) {
             });
             BCK(cudaGetLastError());
         };
-        // forward spectrum passes on the tensor cores: F -> D1 = Ck F^T -> S = D1 Cv^T
+        // forward spectrum passes on the tensor cores: F -> D1 = Ck F^T -> S' = D1 Cv^T,
+        // S' over the distinct |r - N/2| and written to both mirror rows of the window
         auto tc_forward = [&] {
             const size_t sF = (size_t)nF * cm->ldF, sD = (size_t)g.K * cm->ldF;
             sweep_fold_kernel<<<dim3((nF * nF + 255) / 256, B), 256, 0, s>>>(g, intensity, mc, tF, tF + B * sF,
@@ -2359,20 +2370,21 @@ static void batch_run(const BatchCall& call) {
             const tc::Params p1{g.K, nF, nF, tD1, tD1 + B * sD, (long long)sD, cm->ldF, tc::kStoreTf32, 0, 1, &st->err};
             tc_gemm(a1, b1, p1, B, s);
             const tc::Operand a2{tD1, tD1 + B * sD, g.K, nF, cm->ldF, (long long)sD, B};
-            const tc::Operand b2{cm->cv_hi, cm->cv_lo, g.W, nF, cm->ldF, 0, 1};
-            const tc::Params p2{g.K, g.W, nF, reinterpret_cast<float*>(wel), nullptr, (long long)ncell, g.W,
-                                tc::kStore, 1, 0, &st->err};
+            const tc::Operand b2{cm->cv_hi, cm->cv_lo, cm->T1, nF, cm->ldF, 0, 1};
+            tc::Params p2{g.K, cm->T1, nF, reinterpret_cast<float*>(wel), nullptr, (long long)ncell, g.W,
+                          tc::kStoreMirror, 1, 0, &st->err};
+            p2.mirror_h0 = g.N / 2 - g.r0;
             tc_gemm(a2, b2, p2, B, s);
         };
         // adjoint on the tensor cores: window gradient G -> G1 = Cv^T G^T -> dchi2/dF = G1 Ck -> sweep adjoint
         auto tc_adjoint = [&] {
-            const size_t sG = (size_t)g.K * cm->ldW, sG1 = (size_t)nF * cm->ldK, sF = (size_t)nF * cm->ldF;
+            const size_t sG = (size_t)g.K * cm->ldT, sG1 = (size_t)nF * cm->ldK, sF = (size_t)nF * cm->ldF;
             quadT_real_tc_kernel<<<dim3(g.K, B), 256, 0, s>>>(g, cgrad, reinterpret_cast<const float*>(wel), tG,
-                                                              tG + B * sG, cm->ldW);
+                                                              tG + B * sG, cm->T1, cm->ldT);
             BCK(cudaGetLastError());
-            const tc::Operand a1{cm->cvt_hi, cm->cvt_lo, nF, g.W, cm->ldW, 0, 1};
-            const tc::Operand b1{tG, tG + B * sG, g.K, g.W, cm->ldW, (long long)sG, B};
-            const tc::Params p1{nF, g.K, g.W, tG1, tG1 + B * sG1, (long long)sG1, cm->ldK, tc::kStoreTf32, 0, 1,
+            const tc::Operand a1{cm->cvt_hi, cm->cvt_lo, nF, cm->T1, cm->ldT, 0, 1};
+            const tc::Operand b1{tG, tG + B * sG, g.K, cm->T1, cm->ldT, (long long)sG, B};
+            const tc::Params p1{nF, g.K, cm->T1, tG1, tG1 + B * sG1, (long long)sG1, cm->ldK, tc::kStoreTf32, 0, 1,
                                 &st->err};
             tc_gemm(a1, b1, p1, B, s);
             const tc::Operand a2{tG1, tG1 + B * sG1, nF, g.K, cm->ldK, (long long)sG1, B};

@@ -53,8 +53,9 @@ constexpr int kThreads = 192;   // producer warp, MMA warp, four epilogue warps
 constexpr unsigned kErrSpin = 8u;  // the error bit of a wait that ran out (ERR_SPIN of the batched path)
 
 enum Epilogue : int {
-    kStore = 0,    // C = A B^T
-    kStoreTf32 = 1 // C = hi, C2 = lo of the TF32 split of A B^T
+    kStore = 0,     // C = A B^T
+    kStoreTf32 = 1, // C = hi, C2 = lo of the TF32 split of A B^T
+    kStoreMirror = 2  // column t of A B^T to columns h0 - t and h0 + t of C (those in [0, ldc))
 };
 
 struct Params {
@@ -66,6 +67,7 @@ struct Params {
     int mode;
     int a_batched, b_batched;   // 0: the operand is shared by all batch entries
     unsigned* err;              // error word (ERR_SPIN)
+    int mirror_h0 = 0;          // kStoreMirror: the column of t = 0
 };
 
 template <int BN> struct Cfg {
@@ -375,7 +377,18 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (row < p.M) {
             float* crow = p.C + (size_t)z * p.c_stride + (size_t)row * p.ldc;
             float* crow2 = p.C2 ? p.C2 + (size_t)z * p.c_stride + (size_t)row * p.ldc : nullptr;
-            if ((p.ldc & 3) == 0 && (p.c_stride & 3) == 0) {
+            if (p.mode == kStoreMirror) {
+                // an even output: column t holds the values of columns h0 -+ t
+#pragma unroll
+                for (int i = 0; i < BN; ++i) {
+                    const int t = n0 + i;
+                    if (t < p.N) {
+                        const int q1 = p.mirror_h0 - t, q2 = p.mirror_h0 + t;
+                        if (q1 >= 0 && q1 < p.ldc) crow[q1] = acc[i];
+                        if (t > 0 && q2 >= 0 && q2 < p.ldc) crow[q2] = acc[i];
+                    }
+                }
+            } else if ((p.ldc & 3) == 0 && (p.c_stride & 3) == 0) {
                 // 16-byte stores: the row starts 16-byte aligned and col, ldc are multiples of 4
 #pragma unroll
                 for (int i = 0; i < BN; i += 4) {
