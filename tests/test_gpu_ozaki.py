@@ -1,9 +1,10 @@
-"""The bf16 tensor-core level products of the FP64 profile spectrum
+"""The bf16 tensor-core digit products of the FP64 profile spectrum
 (galario_gb300/csrc/gb_ozaki.cuh), tested on their own by
-tests/cpp/ozaki_test.cu: integer digit planes against exact int64 sums
-(bit-exact, including level sums of 2^24 - 2^15, the largest the K <= 511
-bound allows) and FP64 products through the digits against long double
-(error below 2^-50 of K max|a| max|b|)."""
+tests/cpp/ozaki_test.cu: the kernel's per-element integer sums (the eight
+levels of every K tile folded into units of 2^-35 and reduced over the K
+tiles) against int64 arithmetic, bit for bit (ragged tiles, every digit at
++-64, 32 K tiles), and FP64 products through the digits against long
+double (error below 2^-50 of K max|a| max|b|)."""
 import os
 import shutil
 import subprocess
