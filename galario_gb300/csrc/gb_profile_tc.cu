@@ -368,6 +368,13 @@ cudaError_t profile_tc_window(ProfileTc* t, int N, DevState* st, C2<double>* out
         t->smem_attr = true;
     }
     const int grid = num_sms();
+    // a launch that fails after the first product has added to the sums
+    // leaves them for the next call: clear both buffers before reporting it
+    auto failed = [&](cudaError_t err) {
+        (void)cudaMemsetAsync(t->p1.p, 0, t->p1.cap, s);
+        (void)cudaMemsetAsync(t->p2.p, 0, t->p2.cap, s);
+        return err;
+    };
     // D1^T = F C[0:K]^T: rows a < nF, columns k < K (the window)
     oz::Params p1{};
     p1.m_max = nF;
@@ -385,7 +392,7 @@ cudaError_t profile_tc_window(ProfileTc* t, int N, DevState* st, C2<double>* out
     e = launch_dependent(oz_mid_kernel, 2 * grid, kFoldThreads, 0, s, p1, static_cast<const int*>(t->ec.p),
                          static_cast<const int*>(t->ef.p), nF, ldF, (long long)C * ldF,
                          static_cast<unsigned short*>(t->dd.p), static_cast<int*>(t->ed.p));
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess) return failed(e);
     // S'^T = C[0:T+1] D1^T: rows t <= T (the window rows' distances), columns k < K
     oz::Params p2{};
     p2.m_max = C;
@@ -399,11 +406,11 @@ cudaError_t profile_tc_window(ProfileTc* t, int N, DevState* st, C2<double>* out
     p2.P = static_cast<long long*>(t->p2.p);
     p2.err = &st->err;
     e = launch_dependent(oz::ozaki_levels_kernel, grid, oz::kThreads, (size_t)oz::kSmem, s, t->map_ca, t->map_d, p2);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess) return failed(e);
     e = launch_dependent(oz_out_kernel, 2 * grid, 256, 0, s, p2, static_cast<const int*>(t->ed.p),
                          static_cast<const int*>(t->ec.p), N, static_cast<const DevState*>(st), out, amp, s_row,
                          s_col);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess) return failed(e);
     return cudaGetLastError();
 }
 
