@@ -794,10 +794,10 @@ def run_ours(args):
             "parity": {"chi2_f64": chi2_64, "chi2_e2e": e2e_chi2, "chi2_cpu": chi2_cpu,
                        "rel_f64_vs_cpu": abs(chi2_64 - chi2_cpu) / abs(chi2_cpu)},
             # per FP64 step (ncu launch list): extent, the sweep's digits, two
-            # tensor-core level products with the pass between them, the
-            # window and cell records, vis; with GALARIO_TC=0: extent, rows,
-            # cols (+ cell records), vis
-            "gpu_launches": (7 if os.environ.get("GALARIO_TC", "1") != "0" else 4) * args.steps,
+            # tensor-core products with the pass between them, the window,
+            # the cell records, vis; with GALARIO_TC=0: extent, rows, cols,
+            # cell records, vis
+            "gpu_launches": (8 if os.environ.get("GALARIO_TC", "1") != "0" else 5) * args.steps,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
