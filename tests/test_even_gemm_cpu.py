@@ -49,3 +49,38 @@ def test_window_is_two_cosine_products(oracle_port, nxy, inc):
     scale = np.abs(spec).max()
     assert np.abs(spec.imag).max() <= 1e-12 * scale  # real up to rounding
     assert np.abs(S - spec.real).max() <= 1e-12 * scale
+
+
+def test_mirror_folded_products_equal_the_full_window():
+    """The second product over the T1 distinct distances t = |r - N/2| of the
+    window rows, written to rows N/2 - t and N/2 + t, equals the product over
+    all W window rows; and its adjoint over the folded window gradient
+    G'[k][t] = G[k][N/2 - t] + G[k][N/2 + t] (the rows inside the window)
+    equals the adjoint over the full gradient (the batched tensor-core passes,
+    gb_batch.cu)."""
+    rng = np.random.default_rng(7)
+    N, nF, K = 256, 40, 30
+    r0, W = N // 2 - 50, 97            # window rows [r0, r0 + W), not symmetric about N/2
+    h0 = N // 2 - r0
+    T1 = max(N // 2 - r0, r0 + W - 1 - N // 2) + 1
+    w = np.where(np.arange(nF) == 0, 1.0, 2.0)
+    C = lambda t: w[None, :] * np.cos(2 * np.pi * np.outer(t, np.arange(nF)) / N)  # noqa: E731
+    D1 = rng.standard_normal((K, nF))
+    rows = np.abs(r0 + np.arange(W) - N // 2)
+    S_full = D1 @ C(rows).T                        # K x W
+    Sp = D1 @ C(np.arange(T1)).T                   # K x T1
+    S_mirror = np.empty((K, W))
+    for t in range(T1):
+        for q in (h0 - t, h0 + t):
+            if 0 <= q < W:
+                S_mirror[:, q] = Sp[:, t]
+    assert np.allclose(S_mirror, S_full, rtol=0, atol=1e-12 * np.abs(S_full).max())
+    G = rng.standard_normal((K, W))
+    Gp = np.zeros((K, T1))
+    for t in range(T1):
+        for q in sorted({h0 - t, h0 + t}):
+            if 0 <= q < W:
+                Gp[:, t] += G[:, q]
+    adj_full = G @ C(rows)                         # K x nF
+    adj_fold = Gp @ C(np.arange(T1))
+    assert np.allclose(adj_fold, adj_full, rtol=0, atol=1e-12 * np.abs(adj_full).max())
